@@ -1,0 +1,172 @@
+/*
+ * vbm3d_gb300 — C ABI of the GB300 (sm_103a) VBM3D denoiser.
+ *
+ * This is the drop-in boundary for the two denoising passes of tehret/vbm3d.
+ * Every entry point replaces one reference function; the replaced interface
+ * is cited beside each declaration (paths are relative to the reference
+ * project root).  Plain pointers and sizes only; no C++ or torch types.
+ *
+ * Video layout (identical to the reference's VideoSize::index,
+ * src/Utilities/LibVideoT.hpp:88-92): float32, planar per frame,
+ *     index(x, y, t, c) = t*W*H*C + c*W*H + y*W + x.
+ * Flows use the same layout with C = 2 (x displacement, then y):
+ *     fflow frame t holds the motion t -> t+1, bflow frame t-1 holds the
+ *     motion t -> t-1 (src/main.cpp:353-369, src/vbm3d.cpp:1129-1130,1153-1154).
+ * A NULL flow pointer means an all-zero flow, which is what the reference's
+ * CLI builds when no flow file is given (src/main.cpp:353-369).
+ *
+ * Pointer arguments of the vbm3d_gpu_* functions are DEVICE pointers on the
+ * current CUDA device; `stream` is a cudaStream_t (NULL = legacy default
+ * stream).  All calls are stream-ordered and return before the GPU work ends,
+ * except where noted.  vbm3d_run_host takes HOST pointers and synchronises.
+ *
+ * Return value: VBM3D_OK (0) or a vbm3d_status code; vbm3d_last_error()
+ * gives a message for the calling thread's last failure.  The reference's
+ * steps return void and silently return on a bad colour space
+ * (src/vbm3d.cpp:467-468); here that case is VBM3D_ERR_COLOR_SPACE.
+ */
+#ifndef VBM3D_GB300_H
+#define VBM3D_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 2D transform codes, src/vbm3d.cpp:34-35. */
+#define VBM3D_DCT 0u
+#define VBM3D_BIOR 1u
+/* 1D transform codes, src/vbm3d.cpp:36-37.  Only T_3D == VBM3D_HADAMARD
+ * selects the Walsh-Hadamard path; every other value selects Haar
+ * (src/vbm3d.cpp:579-584, :828-833). */
+#define VBM3D_HADAMARD 2u
+#define VBM3D_HAAR 4u
+
+typedef enum vbm3d_status {
+    VBM3D_OK = 0,
+    VBM3D_ERR_INVALID_ARGUMENT = 1, /* NULL pointer, zero size, bad parameter */
+    VBM3D_ERR_UNSUPPORTED = 2,      /* valid for the reference, outside this build's limits */
+    VBM3D_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    VBM3D_ERR_OUT_OF_MEMORY = 4,
+    VBM3D_ERR_COLOR_SPACE = 5,      /* estimate_sigma rejected the channel count */
+    VBM3D_ERR_SIZE_MISMATCH = 6     /* flows / videos of different sizes, src/main.cpp:372-376 */
+} vbm3d_status;
+
+/* Mirror of `struct Parameters`, src/parameters.h:21-58, field for field.
+ * `mc` is the reference's bool; `n` is the tile border it uses only for
+ * OpenMP tiling (src/vbm3d.cpp:474-489), ignored on the GPU. */
+typedef struct vbm3d_params {
+    unsigned k;       /* spatial patch size */
+    unsigned kt;      /* temporal patch size */
+    unsigned p;       /* step between reference patches */
+    unsigned N;       /* maximum number of similar patches */
+    float tau;        /* distance threshold */
+    float d;          /* bias toward the reference position */
+    unsigned Nf;      /* frames searched forward and backward */
+    unsigned Ns;      /* search window in the reference frame */
+    unsigned Npr;     /* search window in the other frames */
+    unsigned Nb;      /* matches kept per frame */
+    unsigned T_2D;    /* VBM3D_DCT or VBM3D_BIOR */
+    unsigned T_3D;    /* VBM3D_HADAMARD or anything else (Haar) */
+    float lambda3D;   /* hard threshold factor (step 1) */
+    int mc;           /* motion-compensated 3D patches */
+    int n;            /* tiling border (CPU-only) */
+} vbm3d_params;
+
+typedef struct vbm3d_dims {
+    unsigned width, height, frames, channels;
+} vbm3d_dims;
+
+/* Limits of this build (a call outside them returns VBM3D_ERR_UNSUPPORTED):
+ * channels in {1, 3}; 2 <= k <= 16; kt == 1 unless noted in the
+ * documentation; N <= 32; Nb <= 8; Ns, Npr odd-or-even <= 15; Nf <= 32. */
+
+/* Default parameters of the reference CLI for step 1 (hard threshold) or
+ * step 2 (Wiener) at noise level sigma, i.e. initializeParameters_1 /
+ * initializeParameters_2 with every option left at its default
+ * (src/main.cpp:35-125, :127-207).  `step` is 1 or 2. */
+int vbm3d_default_params(int step, float sigma, vbm3d_params *out);
+
+/* Per-channel noise levels used by both steps: estimate_sigma
+ * (src/Utilities/Utilities.cpp:282-333) called with the bool color_space
+ * read as an integer, exactly as src/vbm3d.cpp:467 and :697 do. */
+int vbm3d_sigma_table(float sigma, unsigned channels, int color_space, float *sigma_table);
+
+/* Step 1 (hard thresholding) into numerator / denominator.
+ * Replaces vbm3d_1st_step (src/vbm3d.h:38-52, src/vbm3d.cpp:447-654) with
+ * crop == NULL; the FFTW plans have no counterpart.  numerator and
+ * denominator (W*H*F*C floats each) are overwritten, as the reference
+ * resizes and zeroes them (src/vbm3d.cpp:509-515). */
+int vbm3d_gpu_step1(const vbm3d_params *prms, const float *noisy,
+                    const float *fflow, const float *bflow, vbm3d_dims dims,
+                    float sigma, int color_space,
+                    float *numerator, float *denominator, void *stream);
+
+/* Step 2 (Wiener) into numerator / denominator.
+ * Replaces vbm3d_2nd_step (src/vbm3d.h:54-70, src/vbm3d.cpp:676-928) with
+ * crop == NULL.  Block matching runs on `basic`. */
+int vbm3d_gpu_step2(const vbm3d_params *prms, const float *noisy, const float *basic,
+                    const float *fflow, const float *bflow, vbm3d_dims dims,
+                    float sigma, int color_space,
+                    float *numerator, float *denominator, void *stream);
+
+/* out[i] = denominator[i] == 0 ? fallback[i] : numerator[i] / denominator[i]
+ * over `count` floats: the division in run_vbm3d (src/vbm3d.cpp:168-170,
+ * :198-202).  `out` may alias `numerator`. */
+int vbm3d_gpu_normalize(const float *numerator, const float *denominator,
+                        const float *fallback, float *out, size_t count, void *stream);
+
+/* In-place RGB -> YUV (forward != 0) or YUV -> RGB colour transform of a
+ * 3-channel video: VideoUtils::transformColorSpace
+ * (src/Utilities/LibVideoT.hpp:763-888).  One-channel videos are left as
+ * they are, as in the reference. */
+int vbm3d_gpu_color_transform(float *video, vbm3d_dims dims, int forward, void *stream);
+
+/* Both passes with run_vbm3d's single-thread semantics
+ * (src/vbm3d.h:25-35, src/vbm3d.cpp:87-211, :356-376): optional colour
+ * transform of `noisy` (in place, and back at the end), step 1, division
+ * with fallback to noisy, step 2, division with fallback to basic.  A step
+ * whose k is 0 is skipped as in the reference; with prms_1->k == 0 `basic`
+ * is an input.  Device pointers; `noisy`, `basic` and `denoised` hold
+ * W*H*F*C floats. */
+int vbm3d_gpu_run(float sigma, float *noisy, const float *fflow, const float *bflow,
+                  float *basic, float *denoised,
+                  const vbm3d_params *prms_1, const vbm3d_params *prms_2,
+                  int color_space, vbm3d_dims dims, void *stream);
+
+/* vbm3d_gpu_run on HOST buffers: copies noisy (and flows, when not NULL) to
+ * the device, runs both passes, copies basic and denoised back, and waits.
+ * `noisy` is not modified (the reference converts its copy back to RGB).
+ * This is the call a CPU program that used run_vbm3d makes. */
+int vbm3d_run_host(float sigma, const float *noisy, const float *fflow, const float *bflow,
+                   float *basic, float *denoised,
+                   const vbm3d_params *prms_1, const vbm3d_params *prms_2,
+                   int color_space, vbm3d_dims dims);
+
+/* Block matching alone, for every reference patch of the step's grid:
+ * computeSimilarPatches (src/vbm3d.cpp:1082-1197) on `video`, with the
+ * reference grid of ind_initialize (src/Utilities/Utilities.cpp:400-415,
+ * src/vbm3d.cpp:471-489).  For reference r (frames outer, rows, then
+ * columns, as the loops at src/vbm3d.cpp:527-538 visit them):
+ *   indexes[r*N + i], distances[r*N + i] for i < nsimp[r]: the sorted
+ *   matches (patch index = index(x, y, t, 0)); nsx[r]: the returned group
+ *   size (largest power of 2 <= matches under tau).
+ * Any of the three outputs may be NULL.  Returns the number of references
+ * in *n_refs when n_refs is not NULL (call with all outputs NULL to size). */
+int vbm3d_gpu_similar_patches(const vbm3d_params *prms, const float *video,
+                              const float *fflow, const float *bflow, vbm3d_dims dims,
+                              unsigned *indexes, float *distances,
+                              unsigned *nsimp, unsigned *nsx,
+                              size_t *n_refs, void *stream);
+
+/* Number of reference patches of one step's grid (rows x columns x frames). */
+int vbm3d_ref_count(const vbm3d_params *prms, vbm3d_dims dims, size_t *n_refs);
+
+const char *vbm3d_status_string(int status);
+const char *vbm3d_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VBM3D_GB300_H */

@@ -1,0 +1,10 @@
+#!/bin/sh
+# Builds the oracle restatement (test infrastructure) into oracle/_build/.
+# IEEE float arithmetic in source order: no fast-math, no FP contraction.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+mkdir -p "$HERE/_build"
+gcc -std=c99 -O2 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared \
+    -I"$HERE" -I"$HERE/fftw_shim" \
+    "$HERE/vbm3d_oracle.c" "$HERE/fftw_shim/fftw_shim.c" -lm \
+    -o "$HERE/_build/liboracle.so"
