@@ -1,0 +1,101 @@
+"""CPU-side checks of the C ABI: the library loads, exports every symbol the
+header declares, and its host logic (defaults, noise table, grid, argument
+validation) matches the oracle.  No kernel runs here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import vbm3d_gb300 as vb
+from oracle.pyoracle import Oracle
+from vbm3d_gb300._abi import Dims, Params
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "vbm3d_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from vbm3d_gb300 import build
+    build.build()
+    return vb.load()
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(vbm3d_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 12, syms
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_default_params_match_oracle(lib):
+    o = Oracle()
+    for step in (1, 2):
+        for sigma in (5.0, 20.0, 30.0, 30.5, 40.0):
+            assert vb.default_params(step, sigma).as_dict() == o.default_params(step, sigma).as_dict()
+
+
+def test_sigma_table_matches_oracle(lib):
+    o = Oracle()
+    for c in (1, 3):
+        for cs in (False, True):
+            np.testing.assert_array_equal(np.array(vb.sigma_table(25.0, c, cs), np.float32), o.sigma_table(25.0, c, cs))
+
+
+def test_ref_count_matches_oracle_grid(lib):
+    o = Oracle()
+    for (w, h, f) in [(176, 144, 10), (960, 540, 50), (1920, 1080, 30), (33, 17, 3)]:
+        for step, sigma in [(1, 20), (2, 20), (2, 40)]:
+            p = o.default_params(step, sigma)
+            d = Dims(w, h, f, 1)
+            rows, cols = o.grid(p, d)
+            assert vb.ref_count(p, d) == len(rows) * len(cols) * f
+
+
+def status_of(lib, fn, *args):
+    return getattr(lib, fn)(*args)
+
+
+@pytest.mark.parametrize("bad,code", [
+    (dict(kt=2), 2),            # temporal patches not on the GPU yet
+    (dict(T_2D=1, k=7), 1),     # bior1.5 needs k == 8
+    (dict(T_2D=5), 1),
+    (dict(p=0), 1),
+    (dict(N=0), 1),
+    (dict(Nb=0), 1),
+    (dict(N=64), 2),
+    (dict(Ns=17), 2),
+    (dict(k=20, T_2D=0), 2),
+])
+def test_invalid_parameters_rejected_before_any_launch(lib, bad, code):
+    p = vb.default_params(1, 20.0).replace(**bad)
+    fake = C.c_void_p(16)  # never dereferenced: validation fails first
+    rc = lib.vbm3d_gpu_step1(C.byref(p), fake, None, None, Dims(64, 48, 4, 1), 20.0, 0, fake, fake, None)
+    assert rc == code, (rc, lib.vbm3d_last_error())
+    assert lib.vbm3d_last_error()
+
+
+def test_invalid_dims_rejected(lib):
+    p = vb.default_params(1, 20.0)
+    fake = C.c_void_p(16)
+    for d, code in [(Dims(0, 48, 4, 1), 1), (Dims(64, 48, 4, 2), 2), (Dims(64, 48, 4, 4), 2), (Dims(7, 48, 4, 1), 1),
+                    (Dims(60000, 60000, 2, 1), 2)]:
+        rc = lib.vbm3d_gpu_step1(C.byref(p), fake, None, None, d, 20.0, 0, fake, fake, None)
+        assert rc == code, (d.width, d.channels, rc, lib.vbm3d_last_error())
+    # a window too small to hold Nb positions: the reference reads past its end
+    p1 = p.replace(Ns=1)
+    assert lib.vbm3d_gpu_step1(C.byref(p1), fake, None, None, Dims(64, 48, 4, 1), 20.0, 0, fake, fake, None) == 1
+    assert lib.vbm3d_gpu_step1(None, fake, None, None, Dims(64, 48, 4, 1), 20.0, 0, fake, fake, None) == 1
+    assert lib.vbm3d_gpu_step2(C.byref(p), fake, None, None, None, Dims(64, 48, 4, 1), 20.0, 0, fake, fake, None) == 1
+
+
+def test_status_strings(lib):
+    for code in range(7):
+        assert lib.vbm3d_status_string(code).startswith(b"VBM3D_")

@@ -1,0 +1,214 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and
+the golden vectors of the reference's own code.
+
+Tolerances (stated per the acceptance bar of this port):
+  * block matching: bit-exact (indices, distances, group sizes) on the same
+    input video;
+  * step 1 alone and step 2 alone on the same inputs: max |diff| <= 1e-3 on
+    the 0-255 scale (the only source of difference is the order of the
+    float additions of the aggregation, and the float DCT);
+  * end to end (step 2 block matching runs on the GPU's own basic estimate,
+    whose last bits depend on the aggregation order): PSNR within 0.01 dB,
+    and the share of pixels off by more than 1e-3 reported and bounded.
+"""
+import numpy as np
+import pytest
+
+from golden_util import load, names
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import vbm3d_gb300 as vb  # noqa: E402
+from oracle.pyoracle import Oracle  # noqa: E402
+from vbm3d_gb300.synth import make_clip, psnr  # noqa: E402
+
+TOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    vb.load()
+    return torch.device("cuda:0")
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return Oracle()
+
+
+def gpu(a, dev):
+    return None if a is None else torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def gpu_similar(video, p, dev, ff=None, bf=None):
+    res = vb.similar_patches(gpu(video, dev), p, gpu(ff, dev), gpu(bf, dev))
+    torch.cuda.synchronize()
+    out = {k: v.cpu().numpy() for k, v in res.items()}
+    out["idx"] = out["idx"].view(np.uint32)
+    out["nsimp"] = out["nsimp"].astype(np.uint32)
+    out["nsx"] = out["nsx"].astype(np.uint32)
+    return out
+
+
+def assert_bm_equal(got, want, p):
+    np.testing.assert_array_equal(got["nsimp"], want["nsimp"])
+    np.testing.assert_array_equal(got["nsx"], want["nsx"])
+    n = want["nsimp"]
+    mask = np.arange(p.N)[None, :] < n[:, None]
+    np.testing.assert_array_equal(got["idx"][mask], want["idx"][mask])
+    np.testing.assert_array_equal(got["dist"][mask], want["dist"][mask])
+
+
+GPU_CASES = [n for n in names() if "kt2" not in n]
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_block_matching_golden(dev, oracle, name):
+    g = load(name)
+    vid1 = oracle.color_transform(g["noisy"], True) if g["color_space"] else g["noisy"]
+    got = gpu_similar(vid1, g["p1"], dev, g["fflow"], g["bflow"])
+    assert_bm_equal(got, {k: g["bm1_" + k] for k in ("idx", "dist", "nsimp", "nsx")}, g["p1"])
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_block_matching_golden_step2(dev, oracle, name):
+    g = load(name)
+    vid1 = oracle.color_transform(g["noisy"], True) if g["color_space"] else g["noisy"]
+    num, den = oracle.step(1, g["p1"], g["sigma"], vid1, None, g["fflow"], g["bflow"], g["color_space"])
+    basic = np.where(den == 0, vid1, num / np.where(den == 0, 1, den)).astype(np.float32)
+    got = gpu_similar(basic, g["p2"], dev, g["fflow"], g["bflow"])
+    assert_bm_equal(got, {k: g["bm2_" + k] for k in ("idx", "dist", "nsimp", "nsx")}, g["p2"])
+
+
+@pytest.mark.parametrize("shape,sigma,flow,seed", [
+    ((96, 72, 7, 3), 20.0, True, 11),
+    ((120, 64, 9, 1), 40.0, True, 12),
+    ((64, 64, 6, 3), 10.0, False, 13),
+])
+def test_block_matching_synthetic(dev, oracle, shape, sigma, flow, seed):
+    w, h, f, c = shape
+    _, noisy, ff, bf = make_clip(w, h, f, c, sigma, seed, with_flow=flow)
+    for step in (1, 2):
+        p = oracle.default_params(step, sigma)
+        want = oracle.similar(p, noisy, ff, bf)
+        got = gpu_similar(noisy, p, dev, ff, bf)
+        assert_bm_equal(got, want, p)
+
+
+def test_block_matching_ties(dev, oracle):
+    # integer-valued video: exact distance ties everywhere, resolved in the
+    # reference's std::partial_sort order
+    rng = np.random.default_rng(3)
+    vid = np.round(rng.normal(100, 0.8, (6, 1, 40, 48))).astype(np.float32)
+    for p in (oracle.default_params(1, 5.0), oracle.default_params(2, 5.0),
+              oracle.default_params(1, 5.0).replace(Nb=3, N=16, Ns=9)):
+        assert_bm_equal(gpu_similar(vid, p, dev), oracle.similar(p, vid), p)
+    flat = np.full((4, 3, 24, 28), 50.0, np.float32)
+    p = oracle.default_params(1, 5.0)
+    assert_bm_equal(gpu_similar(flat, p, dev), oracle.similar(p, flat), p)
+
+
+def ratio(num, den, fb):
+    return np.where(den == 0, fb, num / np.where(den == 0, 1, den)).astype(np.float32)
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_step1_golden(dev, oracle, name):
+    g = load(name)
+    vid1 = oracle.color_transform(g["noisy"], True) if g["color_space"] else g["noisy"]
+    num, den = vb.step1(gpu(vid1, dev), g["p1"], g["sigma"], gpu(g["fflow"], dev), gpu(g["bflow"], dev),
+                        g["color_space"])
+    torch.cuda.synchronize()
+    onum, oden = oracle.step(1, g["p1"], g["sigma"], vid1, None, g["fflow"], g["bflow"], g["color_space"])
+    b_gpu = ratio(num.cpu().numpy(), den.cpu().numpy(), vid1)
+    b_ora = ratio(onum, oden, vid1)
+    assert np.abs(b_gpu - b_ora).max() <= TOL
+    np.testing.assert_allclose(den.cpu().numpy(), oden, rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_step2_golden_given_oracle_basic(dev, oracle, name):
+    g = load(name)
+    vid1 = oracle.color_transform(g["noisy"], True) if g["color_space"] else g["noisy"]
+    onum, oden = oracle.step(1, g["p1"], g["sigma"], vid1, None, g["fflow"], g["bflow"], g["color_space"])
+    basic = ratio(onum, oden, vid1)
+    num, den = vb.step2(gpu(vid1, dev), gpu(basic, dev), g["p2"], g["sigma"], gpu(g["fflow"], dev),
+                        gpu(g["bflow"], dev), g["color_space"])
+    torch.cuda.synchronize()
+    o2n, o2d = oracle.step(2, g["p2"], g["sigma"], vid1, basic, g["fflow"], g["bflow"], g["color_space"])
+    assert np.abs(ratio(num.cpu().numpy(), den.cpu().numpy(), basic) - ratio(o2n, o2d, basic)).max() <= TOL
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_run_golden(dev, name):
+    g = load(name)
+    x = gpu(g["noisy"], dev)
+    basic, final = vb.run(x, g["sigma"], g["p1"], g["p2"], gpu(g["fflow"], dev), gpu(g["bflow"], dev),
+                          g["color_space"])
+    torch.cuda.synchronize()
+    basic, final = basic.cpu().numpy(), final.cpu().numpy()
+    assert np.abs(basic - g["basic"]).max() <= TOL
+    d = np.abs(final - g["final"])
+    assert (d > TOL).mean() < 0.01, (d.max(), (d > TOL).mean())
+    # the colour transform back is applied to noisy too, as in the reference
+    if g["color_space"]:
+        back = Oracle().color_transform(Oracle().color_transform(g["noisy"], True), False)
+        np.testing.assert_array_equal(x.cpu().numpy(), back)
+
+
+@pytest.mark.parametrize("shape,sigma,cs,seed", [
+    ((176, 144, 10, 1), 20.0, False, 1001),
+    ((96, 80, 8, 3), 30.0, True, 1002),
+    ((96, 80, 8, 3), 40.0, False, 1003),
+])
+def test_psnr_end_to_end(dev, oracle, shape, sigma, cs, seed):
+    w, h, f, c = shape
+    clean, noisy, _, _ = make_clip(w, h, f, c, sigma, seed)
+    p1, p2 = oracle.default_params(1, sigma), oracle.default_params(2, sigma)
+    if shape == (176, 144, 10, 1):
+        p1 = p1.replace(T_2D=0)  # the DCT variant named for the 176x144 gray workload
+    gb, gf = vb.run_host(noisy, sigma, p1, p2, color_space=cs)
+    ob, of = oracle.run(sigma, noisy, p1, p2, color_space=cs, threads=4)
+    assert np.abs(gb - ob).max() <= TOL
+    assert abs(psnr(clean, gf) - psnr(clean, of)) <= 0.01
+    assert abs(psnr(clean, gb) - psnr(clean, ob)) <= 0.01
+    assert psnr(clean, gf) > psnr(clean, noisy) + 5
+
+
+def test_normalize_and_color_exact(dev, oracle):
+    rng = np.random.default_rng(9)
+    v = rng.uniform(-50, 300, (3, 3, 17, 23)).astype(np.float32)
+    num = rng.normal(0, 10, v.shape).astype(np.float32)
+    den = np.where(rng.random(v.shape) < 0.2, 0, rng.uniform(0.1, 3, v.shape)).astype(np.float32)
+    out = vb.normalize(gpu(num, dev), gpu(den, dev), gpu(v, dev)).cpu().numpy()
+    np.testing.assert_array_equal(out, ratio(num, den, v))
+    for fwd in (True, False):
+        t = gpu(v, dev)
+        vb.color_transform(t, fwd)
+        np.testing.assert_array_equal(t.cpu().numpy(), oracle.color_transform(v, fwd))
+
+
+def test_run_host_matches_device_run(dev):
+    _, noisy, ff, bf = make_clip(64, 48, 5, 3, 25.0, 77, with_flow=True)
+    hb, hf = vb.run_host(noisy, 25.0, fflow=ff, bflow=bf, color_space=True)
+    db, df = vb.run(gpu(noisy, dev), 25.0, fflow=gpu(ff, dev), bflow=gpu(bf, dev), color_space=True)
+    torch.cuda.synchronize()
+    assert np.abs(hb - db.cpu().numpy()).max() <= TOL
+    assert np.abs(hf - df.cpu().numpy()).max() <= 0.5
+
+
+def test_skip_steps(dev, oracle):
+    _, noisy, _, _ = make_clip(48, 40, 4, 1, 20.0, 5)
+    p1, p2 = oracle.default_params(1, 20.0), oracle.default_params(2, 20.0)
+    b, f = vb.run_host(noisy, 20.0, p1, p2.replace(k=0))
+    np.testing.assert_array_equal(b, f)
+    ob, _ = oracle.run(20.0, noisy, p1, p2.replace(k=0))
+    assert np.abs(b - ob).max() <= TOL
+    # step 1 skipped: basic is an input (the reference's -b option)
+    b2, f2 = vb.run_host(noisy, 20.0, p1.replace(k=0), p2, basic=ob.copy())
+    np.testing.assert_array_equal(b2, ob)
+    num, den = oracle.step(2, p2, 20.0, noisy, ob)
+    assert np.abs(f2 - ratio(num, den, ob)).max() <= TOL

@@ -1,1 +1,188 @@
-"""GB300-native VBM3D (placeholder; filled in below)."""
+"""GB300-native VBM3D video denoising (sm_103a CUDA kernels behind a C ABI).
+
+The library is libvbm3d_gb300.so (built in-tree by vbm3d_gb300.build); its C
+ABI is include/vbm3d_gb300.h.  This module is a thin ctypes binding over that
+ABI for Python callers, with torch tensors as device buffers.  There is no
+CPU fallback: every call runs the CUDA kernels, and importing a missing or
+stale library raises.
+
+Entry points mirror the reference's hot path (tehret/vbm3d):
+  default_params(step, sigma)        initializeParameters_1/_2 (src/main.cpp:35-207)
+  step1(...), step2(...)             vbm3d_1st_step / vbm3d_2nd_step (src/vbm3d.cpp:447-928)
+  normalize(...)                     run_vbm3d's num/den division (src/vbm3d.cpp:168-202)
+  color_transform(...)               VideoUtils::transformColorSpace
+  similar_patches(...)               computeSimilarPatches over the reference grid
+  run(...) / run_host(...)           run_vbm3d (src/vbm3d.cpp:87-376), device / host buffers
+"""
+import ctypes as C
+import os
+
+from ._abi import BIOR, DCT, HAAR, HADAMARD, STATUS, Dims, Params, dims_of  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libvbm3d_gb300.so")
+
+_fp = C.POINTER(C.c_float)
+_up = C.POINTER(C.c_uint)
+_lib = None
+
+
+class VBM3DError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS.get(status, status), message))
+        self.status = status
+
+
+def load(path=LIB_PATH):
+    """Loads the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libvbm3d_gb300.so is not built: run `python -m vbm3d_gb300.build` "
+                          "(or __graft_entry__.build())")
+    L = C.CDLL(path)
+    P = C.POINTER(Params)
+    vp = C.c_void_p
+    L.vbm3d_default_params.argtypes = [C.c_int, C.c_float, P]
+    L.vbm3d_sigma_table.argtypes = [C.c_float, C.c_uint, C.c_int, _fp]
+    L.vbm3d_ref_count.argtypes = [P, Dims, C.POINTER(C.c_size_t)]
+    L.vbm3d_gpu_step1.argtypes = [P, vp, vp, vp, Dims, C.c_float, C.c_int, vp, vp, vp]
+    L.vbm3d_gpu_step2.argtypes = [P, vp, vp, vp, vp, Dims, C.c_float, C.c_int, vp, vp, vp]
+    L.vbm3d_gpu_normalize.argtypes = [vp, vp, vp, vp, C.c_size_t, vp]
+    L.vbm3d_gpu_color_transform.argtypes = [vp, Dims, C.c_int, vp]
+    L.vbm3d_gpu_run.argtypes = [C.c_float, vp, vp, vp, vp, vp, P, P, C.c_int, Dims, vp]
+    L.vbm3d_run_host.argtypes = [C.c_float, vp, vp, vp, vp, vp, P, P, C.c_int, Dims]
+    L.vbm3d_gpu_similar_patches.argtypes = [P, vp, vp, vp, Dims, vp, vp, vp, vp, C.POINTER(C.c_size_t), vp]
+    L.vbm3d_status_string.restype = C.c_char_p
+    L.vbm3d_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise VBM3DError(rc, load().vbm3d_last_error().decode())
+
+
+def default_params(step, sigma):
+    p = Params()
+    _check(load().vbm3d_default_params(step, sigma, C.byref(p)))
+    return p
+
+
+def sigma_table(sigma, channels, color_space):
+    out = (C.c_float * 3)()
+    _check(load().vbm3d_sigma_table(sigma, channels, int(color_space), out))
+    return list(out)[:channels]
+
+
+def ref_count(params, dims):
+    n = C.c_size_t()
+    _check(load().vbm3d_ref_count(C.byref(params), dims, C.byref(n)))
+    return n.value
+
+
+# ---------------------------------------------------------------- torch ---
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _video(t, name):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()
+            and t.dim() == 4):
+        raise TypeError("%s must be a contiguous float32 CUDA tensor [F, C, H, W]" % name)
+    return t
+
+
+def _dims(t):
+    f, c, h, w = t.shape
+    return Dims(w, h, f, c)
+
+
+def step1(noisy, params, sigma, fflow=None, bflow=None, color_space=False, out=None, stream=None):
+    """vbm3d_1st_step on the GPU: returns (numerator, denominator)."""
+    import torch
+    _video(noisy, "noisy")
+    num, den = out if out is not None else (torch.empty_like(noisy), torch.empty_like(noisy))
+    _check(load().vbm3d_gpu_step1(C.byref(params), _ptr(noisy), _ptr(fflow), _ptr(bflow), _dims(noisy), sigma,
+                                  int(color_space), _ptr(num), _ptr(den), _stream(stream)))
+    return num, den
+
+
+def step2(noisy, basic, params, sigma, fflow=None, bflow=None, color_space=False, out=None, stream=None):
+    """vbm3d_2nd_step on the GPU: returns (numerator, denominator)."""
+    import torch
+    _video(noisy, "noisy")
+    _video(basic, "basic")
+    num, den = out if out is not None else (torch.empty_like(noisy), torch.empty_like(noisy))
+    _check(load().vbm3d_gpu_step2(C.byref(params), _ptr(noisy), _ptr(basic), _ptr(fflow), _ptr(bflow),
+                                  _dims(noisy), sigma, int(color_space), _ptr(num), _ptr(den), _stream(stream)))
+    return num, den
+
+
+def normalize(num, den, fallback, out=None, stream=None):
+    import torch
+    out = torch.empty_like(num) if out is None else out
+    _check(load().vbm3d_gpu_normalize(_ptr(num), _ptr(den), _ptr(fallback), _ptr(out), num.numel(),
+                                      _stream(stream)))
+    return out
+
+
+def color_transform(video, forward, stream=None):
+    """In place."""
+    _video(video, "video")
+    _check(load().vbm3d_gpu_color_transform(_ptr(video), _dims(video), int(forward), _stream(stream)))
+    return video
+
+
+def similar_patches(video, params, fflow=None, bflow=None, stream=None):
+    """Block matching for every reference patch of the step's grid.
+    Returns dict(idx [R, N] int32 view of u32, dist [R, N], nsimp [R], nsx [R])."""
+    import torch
+    _video(video, "video")
+    d = _dims(video)
+    n = ref_count(params, d)
+    dev = video.device
+    idx = torch.empty((n, params.N), dtype=torch.int32, device=dev)
+    dist = torch.empty((n, params.N), dtype=torch.float32, device=dev)
+    nsimp = torch.empty(n, dtype=torch.int32, device=dev)
+    nsx = torch.empty(n, dtype=torch.int32, device=dev)
+    _check(load().vbm3d_gpu_similar_patches(C.byref(params), _ptr(video), _ptr(fflow), _ptr(bflow), d, _ptr(idx),
+                                            _ptr(dist), _ptr(nsimp), _ptr(nsx), None, _stream(stream)))
+    return dict(idx=idx, dist=dist, nsimp=nsimp, nsx=nsx)
+
+
+def run(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=False, stream=None):
+    """run_vbm3d on device buffers.  `noisy` is transformed in place and back
+    (as the reference does).  Returns (basic, denoised)."""
+    import torch
+    _video(noisy, "noisy")
+    p1 = default_params(1, sigma) if p1 is None else p1
+    p2 = default_params(2, sigma) if p2 is None else p2
+    basic, den = torch.empty_like(noisy), torch.empty_like(noisy)
+    _check(load().vbm3d_gpu_run(sigma, _ptr(noisy), _ptr(fflow), _ptr(bflow), _ptr(basic), _ptr(den),
+                                C.byref(p1), C.byref(p2), int(color_space), _dims(noisy), _stream(stream)))
+    return basic, den
+
+
+def run_host(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=False, basic=None, out=None):
+    """run_vbm3d on host (numpy) arrays: copies in, denoises, copies out."""
+    import numpy as np
+    noisy = np.ascontiguousarray(noisy, dtype=np.float32)
+    p1 = default_params(1, sigma) if p1 is None else p1
+    p2 = default_params(2, sigma) if p2 is None else p2
+    basic = np.empty_like(noisy) if basic is None else basic
+    out = np.empty_like(noisy) if out is None else out
+    vp = lambda a: None if a is None else C.c_void_p(a.ctypes.data)  # noqa: E731
+    _check(load().vbm3d_run_host(sigma, vp(noisy), vp(fflow), vp(bflow), vp(basic), vp(out), C.byref(p1),
+                                 C.byref(p2), int(color_space), dims_of(noisy)))
+    return basic, out

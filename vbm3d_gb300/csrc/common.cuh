@@ -1,0 +1,157 @@
+// Shared definitions of the GB300 VBM3D kernels.
+//
+// Video layout (the reference's VideoSize::index, src/Utilities/LibVideoT.hpp:88-92):
+//   index(x, y, t, c) = t*W*H*C + c*W*H + y*W + x, float32.
+// A patch is named by the index of its top-left pixel in channel 0, exactly
+// as the reference names it (src/vbm3d.cpp:546, :1062).
+//
+// This file is compiled with --fmad=false: every a*b+c written in the
+// kernels rounds the product and the sum separately, as the reference's C++
+// does when built without fast-math, so block-matching distances, the
+// bior1.5 passes and the shrinkage decisions reproduce the reference's float
+// arithmetic operation by operation.  FMAs are written explicitly
+// (__fmaf_rn) only where the reference's value is not reproducible anyway
+// (the DCT, whose reference value comes from FFTW's own float codelets).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vbm3d {
+
+constexpr int kMaxK = 16;        // patch side
+constexpr int kMaxN = 32;        // similar patches per group
+constexpr int kMaxNb = 8;        // matches kept per frame
+constexpr int kMaxWin = 15;      // search window side (Ns, Npr)
+constexpr int kMaxNf = 16;       // frames searched each way
+constexpr int kMaxC = 3;         // channels
+constexpr int kSlots = 8;        // window candidates per lane: 32*8 >= 15*15
+constexpr unsigned kFull = 0xffffffffu;
+
+// bior1.5 / DCT codes of the reference (src/vbm3d.cpp:34-37).
+constexpr int kDCT = 0;
+constexpr int kBIOR = 1;
+constexpr int kHADAMARD = 2;
+
+// sqrt(1/2) as the reference's double literal SQRT2_INV
+// (src/vbm3d.cpp:33), split into a float head and a float tail so that
+// fmaf(s, kS2iHi, s * kS2iLo) rounds s * SQRT2_INV to float the way the
+// reference's (float)((double)s * SQRT2_INV) does.
+constexpr float kS2iHi = 0.70710676908493042f;          // float(0.7071067811865475)
+constexpr float kS2iLo = 1.2101617485882343e-08f;       // float(0.7071067811865475 - kS2iHi)
+
+// Everything a step kernel needs, passed by value (a few KB of kernel
+// parameter space).
+struct StepParams {
+    // video
+    int W, H, F, C;
+    unsigned wh, whc;
+    // algorithm parameters (struct Parameters, src/parameters.h:21-58)
+    int k, kt, p, N, Nf, Ns, Npr, Nb, T2D, T3D, mc;
+    float tau, dbias, lambda3D;
+    // reference grid (ind_initialize, src/Utilities/Utilities.cpp:400-415)
+    int nrows, ncols, nframes;
+    long long nrefs;
+    long long ref_base;         // first reference of this launch (chunking)
+    // noise per channel (estimate_sigma)
+    float sigma[kMaxC];
+    // tables (k*k each, row-major)
+    float kaiser[kMaxK * kMaxK];
+    float fwd[kMaxK * kMaxK];   // DCT: 2cos(pi (j+1/2) u / k) [u][j]; bior: basis rows
+    float inv[kMaxK * kMaxK];   // DCT: REDFT01 matrix [i][u]; bior: inverse basis rows
+    float cn[kMaxK * kMaxK];    // DCT normalisation (preProcess, src/vbm3d.cpp:1843-1863)
+    float cni[kMaxK * kMaxK];
+    // block-matching shared-memory layout (floats / pairs per warp)
+    int bm_list_cap, bm_best_cap, bm_win_cap, bm_warp_bytes;
+};
+
+// Reference r of the grid, frames outer, then rows, then columns
+// (the loop order of src/vbm3d.cpp:527-538).
+__device__ __forceinline__ void ref_coords(const StepParams& P, long long r, int& x, int& y, int& t)
+{
+    const long long per_frame = (long long)P.nrows * P.ncols;
+    t = (int)(r / per_frame);
+    const int rem = (int)(r - (long long)t * per_frame);
+    const int ir = rem / P.ncols, jr = rem - ir * P.ncols;
+    y = min(ir * P.p, P.H - P.k);
+    x = min(jr * P.p, P.W - P.k);
+}
+
+__device__ __forceinline__ unsigned patch_index(const StepParams& P, int x, int y, int t)
+{
+    return (unsigned)t * P.whc + (unsigned)y * (unsigned)P.W + (unsigned)x;
+}
+
+__device__ __forceinline__ void patch_coords(const StepParams& P, unsigned idx, int& x, int& y, int& t)
+{
+    t = (int)(idx / P.whc);
+    const unsigned r = idx - (unsigned)t * P.whc;   // channel 0: r < wh
+    y = (int)(r / (unsigned)P.W);
+    x = (int)(r - (unsigned)y * (unsigned)P.W);
+}
+
+// (float)((double)s * SQRT2_INV) with float arithmetic (see kS2iHi).
+__device__ __forceinline__ float mul_sqrt2_inv(float s)
+{
+    return __fmaf_rn(s, kS2iHi, __fmul_rn(s, kS2iLo));
+}
+
+struct Pair {
+    float d;
+    unsigned i;
+};
+
+// libstdc++ std::partial_sort (GCC 13: bits/stl_algo.h __partial_sort /
+// __heap_select, bits/stl_heap.h __make_heap / __adjust_heap / __push_heap /
+// __pop_heap / __sort_heap) with the reference's comparator
+// (a.first < b.first, src/Utilities/Utilities.cpp:40-45).  One thread.
+// Reproducing it keeps the reference's order among equal distances.
+__device__ __forceinline__ void heap_adjust(Pair* a, int hole, int len, Pair value)
+{
+    const int top = hole;
+    int child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (a[child].d < a[child - 1].d) child--;
+        a[hole] = a[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        a[hole] = a[child - 1];
+        hole = child - 1;
+    }
+    int parent = (hole - 1) / 2;
+    while (hole > top && a[parent].d < value.d) {
+        a[hole] = a[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    a[hole] = value;
+}
+
+__device__ __forceinline__ void heap_pop(Pair* a, int len, int result)
+{
+    Pair v = a[result];
+    a[result] = a[0];
+    heap_adjust(a, 0, len, v);
+}
+
+__device__ inline void partial_sort(Pair* a, int middle, int last)
+{
+    if (middle <= 0) return;
+    if (middle >= 2) {
+        for (int parent = (middle - 2) / 2;; parent--) {
+            heap_adjust(a, parent, middle, a[parent]);
+            if (parent == 0) break;
+        }
+    }
+    for (int i = middle; i < last; ++i)
+        if (a[i].d < a[0].d) heap_pop(a, middle, i);
+    for (int l = middle; l > 1;) {
+        --l;
+        heap_pop(a, l, l);
+    }
+}
+
+}  // namespace vbm3d

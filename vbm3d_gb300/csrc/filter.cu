@@ -1,0 +1,397 @@
+// K-T + K-A: collaborative filtering of one group and its aggregation.
+//
+// Replaces, for one reference patch, dct_2d_process / bior_2d_process
+// (src/vbm3d.cpp:1218-1386), the regrouping (:565-570), ht_filtering_* and
+// wiener_filtering_* (:1405-1666), dct_2d_inv / bior_2d_inv (:1678-1731) and
+// the aggregation loops (:612-650, :860-924).  One warp handles one group:
+//
+//  * the nsx patches of every channel are gathered into shared memory as
+//    slices [c][n][k*k] (slice stride k*k + 1 to spread banks);
+//  * the 2D transform runs one slice per lane: bior1.5 as the reference's
+//    two basis-matrix passes in its float order (bit-identical), the DCT as
+//    two float matrix passes followed by the reference's normalisation;
+//  * the 1D Haar (or Walsh-Hadamard) transform along the group runs one
+//    coefficient vector per lane, in registers, with the reference's
+//    rounding, then hard thresholding (group DC always kept) or Wiener
+//    shrinkage, then the inverse;
+//  * per-channel weights follow the reference's formulas; the inverse 2D
+//    transform runs one slice per lane and every pixel is added into the
+//    numerator / denominator with a Kaiser window weight by red.global.add.
+#include "common.cuh"
+
+namespace vbm3d {
+
+// ---------------------------------------------------------------- 2D ---
+
+// bior_2d_forward passes (src/lib_transforms.cpp:158-176): t[i][j] =
+// sum_k x[i][k] B[j][k]; x[i][j] = sum_k t[k][i] B[j][k]; sums from k = 0.
+__device__ __forceinline__ void bior_fwd8(float* x, float* t, const float* B)
+{
+    for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+            float m = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; q++) m = m + x[i * 8 + q] * B[j * 8 + q];
+            t[i * 8 + j] = m;
+        }
+    for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+            float m = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; q++) m = m + t[q * 8 + i] * B[j * 8 + q];
+            x[i * 8 + j] = m;
+        }
+}
+
+// bior_2d_inverse (src/lib_transforms.cpp:294-320): transposed read, the
+// same two passes with the inverse basis, transposed write.
+__device__ __forceinline__ void bior_inv8(float* x, float* t, const float* B)
+{
+    for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+            float m = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; q++) m = m + x[i + q * 8] * B[j * 8 + q];
+            t[i * 8 + j] = m;
+        }
+    for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+            float m = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; q++) m = m + t[q * 8 + i] * B[j * 8 + q];
+            x[j * 8 + i] = m;
+        }
+}
+
+// Orthonormal 2D DCT-II of a k x k block: FFTW REDFT10 along rows and
+// columns, Y = D X D^T with D[u][j] = 2cos(pi (j + 1/2) u / k), then the
+// reference's normalisation Y[u][v] * coef_norm[u*k + v] (src/vbm3d.cpp:1294-1302).
+__device__ __forceinline__ void dct_fwd(float* x, float* t, const StepParams& P)
+{
+    const int k = P.k;
+    for (int i = 0; i < k; i++)
+        for (int v = 0; v < k; v++) {
+            float m = 0.f;
+            for (int j = 0; j < k; j++) m = __fmaf_rn(x[i * k + j], P.fwd[v * k + j], m);
+            t[i * k + v] = m;
+        }
+    for (int u = 0; u < k; u++)
+        for (int v = 0; v < k; v++) {
+            float m = 0.f;
+            for (int i = 0; i < k; i++) m = __fmaf_rn(P.fwd[u * k + i], t[i * k + v], m);
+            x[u * k + v] = m * P.cn[u * k + v];
+        }
+}
+
+// dct_2d_inv (src/vbm3d.cpp:1696-1709): Z = Y * coef_norm_inv, REDFT01 along
+// both axes (X = E Z E^T, E[i][u] = u ? 2cos(pi u (i + 1/2) / k) : 1), times 1/(2k).
+__device__ __forceinline__ void dct_inv(float* x, float* t, const StepParams& P)
+{
+    const int k = P.k;
+    const float coef = 1.0f / (float)(k * 2);
+    for (int u = 0; u < k; u++)
+        for (int j = 0; j < k; j++) {
+            float m = 0.f;
+            for (int v = 0; v < k; v++) m = __fmaf_rn(x[u * k + v] * P.cni[u * k + v], P.inv[j * k + v], m);
+            t[u * k + j] = m;
+        }
+    for (int i = 0; i < k; i++)
+        for (int j = 0; j < k; j++) {
+            float m = 0.f;
+            for (int u = 0; u < k; u++) m = __fmaf_rn(P.inv[i * k + u], t[u * k + j], m);
+            x[i * k + j] = coef * m;
+        }
+}
+
+__device__ __forceinline__ void fwd2d(float* x, float* t, const StepParams& P)
+{
+    if (P.T2D == kBIOR) bior_fwd8(x, t, P.fwd);
+    else dct_fwd(x, t, P);
+}
+
+__device__ __forceinline__ void inv2d(float* x, float* t, const StepParams& P)
+{
+    if (P.T2D == kBIOR) bior_inv8(x, t, P.inv);
+    else dct_inv(x, t, P);
+}
+
+// ---------------------------------------------------------------- 1D ---
+
+// haar_forward / haar_inverse (src/lib_transforms.cpp:453-512).
+template <int N>
+__device__ __forceinline__ void haar_fwd(float* v)
+{
+    float tmp[N > 1 ? N : 1];
+#pragma unroll
+    for (int k = N / 2; k >= 1; k /= 2) {
+#pragma unroll
+        for (int i = 0; i < k; i++) {
+            tmp[i] = mul_sqrt2_inv(v[2 * i] + v[2 * i + 1]);
+            tmp[i + k] = mul_sqrt2_inv(v[2 * i] - v[2 * i + 1]);
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void haar_inv(float* v)
+{
+    float tmp[N > 1 ? N : 1];
+#pragma unroll
+    for (int k = 1; k * 2 <= N; k *= 2) {
+#pragma unroll
+        for (int i = 0; i < k; i++) {
+            tmp[2 * i] = mul_sqrt2_inv(v[i] + v[i + k]);
+            tmp[2 * i + 1] = mul_sqrt2_inv(v[i] - v[i + k]);
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
+    }
+}
+
+// hadamard_transform (src/lib_transforms.cpp:410-440), unnormalised; the
+// recursion pairs (2k, 2k+1) into (k, n/2 + k) at every level.
+template <int N>
+__device__ __forceinline__ void hadamard(float* v)
+{
+    if (N == 1) return;
+    float tmp[N > 1 ? N : 1];
+#pragma unroll
+    for (int k = 0; k < N / 2; k++) {
+        tmp[k] = v[2 * k] + v[2 * k + 1];
+        tmp[N / 2 + k] = v[2 * k] - v[2 * k + 1];
+    }
+    hadamard<(N / 2 > 0 ? N / 2 : 1)>(tmp);
+    hadamard<(N / 2 > 0 ? N / 2 : 1)>(tmp + N / 2);
+#pragma unroll
+    for (int k = 0; k < N; k++) v[k] = tmp[k];
+}
+template <>
+__device__ __forceinline__ void hadamard<1>(float*) {}
+
+// Step 1 shrinkage of one coefficient vector (all n at one (c, pq)):
+// ht_filtering_haar / _hadamard (src/vbm3d.cpp:1405-1521).  Returns the
+// number of kept coefficients.
+template <int N>
+__device__ __forceinline__ int ht_vector(float* g, int stride, bool is_dc_pos, float T, int T3D)
+{
+    float v[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) v[n] = g[n * stride];
+    int kept = 0;
+    if (T3D == kHADAMARD) {
+        hadamard<N>(v);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            if ((is_dc_pos && n == 0) || fabsf(v[n]) > T) kept++;
+            else v[n] = 0.0f;
+        }
+        hadamard<N>(v);
+        const float coef = 1.0f / (float)N;
+#pragma unroll
+        for (int n = 0; n < N; n++) v[n] = v[n] * coef;
+    } else {
+        haar_fwd<N>(v);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            if ((is_dc_pos && n == 0) || fabsf(v[n]) > T) kept++;
+            else v[n] = 0.0f;
+        }
+        haar_inv<N>(v);
+    }
+#pragma unroll
+    for (int n = 0; n < N; n++) g[n * stride] = v[n];
+    return kept;
+}
+
+// Step 2 shrinkage: wiener_filtering_haar / _hadamard
+// (src/vbm3d.cpp:1539-1666, DCWIENER on).  Writes the estimate into gb and
+// returns the sum of squared Wiener coefficients.
+template <int N>
+__device__ __forceinline__ float wiener_vector(const float* gn, float* gb, int stride, float s2, int T3D)
+{
+    float vn[N], vb[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+        vn[n] = gn[n * stride];
+        vb[n] = gb[n * stride];
+    }
+    float wsum = 0.f;
+    if (T3D == kHADAMARD) {
+        hadamard<N>(vn);
+        hadamard<N>(vb);
+        const float coef = 1.0f / (float)N;
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            float value = vb[n] * vb[n] * coef;
+            value = value / (value + s2);
+            vb[n] = vn[n] * value * coef;
+            wsum = wsum + value * value;
+        }
+        hadamard<N>(vb);
+    } else {
+        haar_fwd<N>(vn);
+        haar_fwd<N>(vb);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            float value = vb[n] * vb[n];
+            value = value / (value + s2);
+            vb[n] = vn[n] * value;
+            wsum = wsum + value * value;
+        }
+        haar_inv<N>(vb);
+    }
+#pragma unroll
+    for (int n = 0; n < N; n++) gb[n * stride] = vb[n];
+    return wsum;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+    return v;
+}
+
+// Gather the nsx patches of all channels of `vid` into slices [c][n][k*k].
+__device__ __forceinline__ void gather(const StepParams& P, const float* __restrict__ vid,
+                                       const unsigned* idx, int nsx, int ss, float* g, int lane)
+{
+    const int k = P.k, k2 = k * k;
+    const int total = P.C * nsx * k2;
+    for (int e = lane; e < total; e += 32) {
+        const int sl = e / k2, pq = e - sl * k2;
+        const int c = sl / nsx, n = sl - c * nsx;
+        const int p = pq / k, q = pq - p * k;
+        int x, y, t;
+        patch_coords(P, idx[n], x, y, t);
+        g[sl * ss + pq] = __ldg(vid + (size_t)t * P.whc + (size_t)c * P.wh + (size_t)(y + p) * P.W + x + q);
+    }
+}
+
+template <int STEP>
+__global__ void __launch_bounds__(128)
+filter_kernel(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
+              const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
+              float* __restrict__ num, float* __restrict__ den, int warp_floats)
+{
+    extern __shared__ __align__(16) float fsm[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    if (r >= P.nrefs) return;
+
+    const int k = P.k, k2 = k * k, C = P.C;
+    const int ss = k2 + 1;  // slice stride
+    float* base = fsm + (size_t)wid * warp_floats;
+    unsigned* idx = reinterpret_cast<unsigned*>(base);
+    float* gA = base + kMaxN;                 // noisy group (step 1: the group)
+    float* gT = gA + (size_t)C * P.N * ss;    // per-slice scratch
+    float* gB = gT + (size_t)C * P.N * ss;    // basic group (step 2)
+
+    const int nsx = (int)tab_nsx[r];
+    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
+    __syncwarp();
+
+    gather(P, noisy, idx, nsx, ss, gA, lane);
+    if (STEP == 2) gather(P, basic, idx, nsx, ss, gB, lane);
+    __syncwarp();
+    const int nsl = C * nsx;
+    for (int sl = lane; sl < nsl; sl += 32) {
+        fwd2d(gA + sl * ss, gT + sl * ss, P);
+        if (STEP == 2) fwd2d(gB + sl * ss, gT + sl * ss, P);
+    }
+    __syncwarp();
+
+    // 1D transform along the group + shrinkage, one (c, pq) per lane
+    float acc[kMaxC] = {0.f, 0.f, 0.f};
+    for (int v = lane; v < C * k2; v += 32) {
+        const int c = v / k2, pq = v - c * k2;
+        float* ga = gA + (size_t)(c * nsx) * ss + pq;
+        float* gb = gB + (size_t)(c * nsx) * ss + pq;
+        if (STEP == 1) {
+            const float T = P.lambda3D * P.sigma[c] * (P.T3D == kHADAMARD ? sqrtf((float)nsx) : 1.0f);
+            int kept;
+            switch (nsx) {
+                case 1: kept = ht_vector<1>(ga, ss, pq == 0, T, P.T3D); break;
+                case 2: kept = ht_vector<2>(ga, ss, pq == 0, T, P.T3D); break;
+                case 4: kept = ht_vector<4>(ga, ss, pq == 0, T, P.T3D); break;
+                case 8: kept = ht_vector<8>(ga, ss, pq == 0, T, P.T3D); break;
+                case 16: kept = ht_vector<16>(ga, ss, pq == 0, T, P.T3D); break;
+                default: kept = ht_vector<32>(ga, ss, pq == 0, T, P.T3D); break;
+            }
+            acc[c] += (float)kept;
+        } else {
+            const float s2 = P.sigma[c] * P.sigma[c];
+            float ws;
+            switch (nsx) {
+                case 1: ws = wiener_vector<1>(ga, gb, ss, s2, P.T3D); break;
+                case 2: ws = wiener_vector<2>(ga, gb, ss, s2, P.T3D); break;
+                case 4: ws = wiener_vector<4>(ga, gb, ss, s2, P.T3D); break;
+                case 8: ws = wiener_vector<8>(ga, gb, ss, s2, P.T3D); break;
+                case 16: ws = wiener_vector<16>(ga, gb, ss, s2, P.T3D); break;
+                default: ws = wiener_vector<32>(ga, gb, ss, s2, P.T3D); break;
+            }
+            acc[c] += ws;
+        }
+    }
+    float wgt[kMaxC];
+#pragma unroll
+    for (int c = 0; c < kMaxC; c++) {
+        const float tot = warp_sum(acc[c]);  // counts are exact; Wiener sums reassociate
+        const float s2 = P.sigma[c] * P.sigma[c];
+        if (STEP == 2 && P.T3D == kHADAMARD) wgt[c] = tot > 0.0f ? 1.0f / (float)(s2 * tot) : 1.0f;
+        else wgt[c] = 1.f / (float)(s2 * tot);
+    }
+    __syncwarp();
+
+    float* ge = STEP == 1 ? gA : gB;
+    for (int sl = lane; sl < nsl; sl += 32) inv2d(ge + sl * ss, gT + sl * ss, P);
+    __syncwarp();
+
+    // aggregation (src/vbm3d.cpp:612-650): num += kaiser * w * est; den += kaiser * w
+    const int total = nsl * k2;
+    for (int e = lane; e < total; e += 32) {
+        const int sl = e / k2, pq = e - sl * k2;
+        const int c = sl / nsx, n = sl - c * nsx;
+        const int p = pq / k, q = pq - p * k;
+        int x, y, t;
+        patch_coords(P, idx[n], x, y, t);
+        const size_t o = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)(y + p) * P.W + x + q;
+        const float kw = P.kaiser[pq] * wgt[c];
+        atomicAdd(num + o, kw * ge[sl * ss + pq]);
+        atomicAdd(den + o, kw);
+    }
+}
+
+int filter_warp_floats(const StepParams& P, int step)
+{
+    const int ss = P.k * P.k + 1;
+    const int groups = step == 1 ? 2 : 3;  // group(s) + scratch
+    return kMaxN + groups * P.C * P.N * ss;
+}
+
+cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
+                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den,
+                          long long count, cudaStream_t stream)
+{
+    const int warps = 4;
+    const int wf = filter_warp_floats(P, step);
+    const size_t smem = (size_t)warps * wf * sizeof(float);
+    const long long blocks = (count + warps - 1) / warps;
+    cudaError_t e;
+    if (step == 1) {
+        e = cudaFuncSetAttribute(filter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        filter_kernel<1><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx, tab_nsx, num,
+                                                                        den, wf);
+    } else {
+        e = cudaFuncSetAttribute(filter_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        filter_kernel<2><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx, tab_nsx, num,
+                                                                        den, wf);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace vbm3d

@@ -1,0 +1,85 @@
+// K-N: numerator / denominator division and the colour transforms.
+// Both are elementwise and HBM-bound: grid-stride loops over float4 where
+// the pointers allow it.
+#include "common.cuh"
+
+namespace vbm3d {
+
+// run_vbm3d's division (src/vbm3d.cpp:168-170, :198-202).
+__global__ void normalize_kernel(const float* num, const float* __restrict__ den,
+                                 const float* __restrict__ fb, float* out, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool vec = ((reinterpret_cast<uintptr_t>(num) | reinterpret_cast<uintptr_t>(den) |
+                       reinterpret_cast<uintptr_t>(fb) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+    if (vec) {
+        const size_t n4 = n / 4;
+        for (size_t j = i; j < n4; j += stride) {
+            const float4 a = reinterpret_cast<const float4*>(num)[j];
+            const float4 b = reinterpret_cast<const float4*>(den)[j];
+            const float4 f = reinterpret_cast<const float4*>(fb)[j];
+            float4 o;
+            o.x = b.x == 0 ? f.x : a.x / b.x;
+            o.y = b.y == 0 ? f.y : a.y / b.y;
+            o.z = b.z == 0 ? f.z : a.z / b.z;
+            o.w = b.w == 0 ? f.w : a.w / b.w;
+            reinterpret_cast<float4*>(out)[j] = o;
+        }
+        for (size_t j = n4 * 4 + i; j < n; j += stride) out[j] = den[j] == 0 ? fb[j] : num[j] / den[j];
+    } else {
+        for (size_t j = i; j < n; j += stride) out[j] = den[j] == 0 ? fb[j] : num[j] / den[j];
+    }
+}
+
+// transformColorSpace, 3 channels (src/Utilities/LibVideoT.hpp:763-888);
+// float operations in the reference's order.
+__global__ void color_kernel(float* __restrict__ v, unsigned wh, unsigned frames, int forward)
+{
+    const size_t n = (size_t)wh * frames;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = i / wh, k = i - f * wh;
+        float* r = v + f * 3 * (size_t)wh + k;
+        float* g = r + wh;
+        float* b = g + wh;
+        const float R = *r, G = *g, B = *b;
+        float o0, o1, o2;
+        if (forward) {
+            o0 = 0.299f * R + 0.587f * G + 0.114f * B;
+            o1 = -0.14713f * R - 0.28886f * G + 0.436f * B;
+            o2 = 0.615f * R - 0.51498f * G - 0.10001f * B;
+        } else {
+            o0 = R + 1.13983f * B;
+            o1 = R - 0.39465f * G - 0.5806f * B;
+            o2 = R + 2.03211f * G;
+        }
+        *r = o0;
+        *g = o1;
+        *b = o2;
+    }
+}
+
+static int grid_for(size_t n, int threads)
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t want = (n + threads - 1) / threads;
+    const size_t cap = (size_t)sms * 8;  // 8 resident blocks of 256 threads per SM
+    return (int)(want < cap ? (want ? want : 1) : cap);
+}
+
+cudaError_t launch_normalize(const float* num, const float* den, const float* fb, float* out, size_t n,
+                             cudaStream_t s)
+{
+    normalize_kernel<<<grid_for(n / 4 + 1, 256), 256, 0, s>>>(num, den, fb, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_color(float* v, unsigned wh, unsigned frames, int forward, cudaStream_t s)
+{
+    color_kernel<<<grid_for((size_t)wh * frames, 256), 256, 0, s>>>(v, wh, frames, forward);
+    return cudaGetLastError();
+}
+
+}  // namespace vbm3d
