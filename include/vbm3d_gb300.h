@@ -160,6 +160,14 @@ int vbm3d_gpu_similar_patches(const vbm3d_params *prms, const float *video,
                               unsigned *nsimp, unsigned *nsx,
                               size_t *n_refs, void *stream);
 
+/* Measurement helper with no reference counterpart: runs the block
+ * matching of vbm3d_gpu_similar_patches and returns in *count the total
+ * number of patch distances it evaluated (calls of the reference's
+ * patchDistance, src/vbm3d.cpp:1068).  Synchronises `stream`. */
+int vbm3d_gpu_bm_distance_count(const vbm3d_params *prms, const float *video,
+                                const float *fflow, const float *bflow, vbm3d_dims dims,
+                                unsigned long long *count, void *stream);
+
 /* Number of reference patches of one step's grid (rows x columns x frames). */
 int vbm3d_ref_count(const vbm3d_params *prms, vbm3d_dims dims, size_t *n_refs);
 

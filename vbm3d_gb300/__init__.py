@@ -54,6 +54,7 @@ def load(path=LIB_PATH):
     L.vbm3d_gpu_run.argtypes = [C.c_float, vp, vp, vp, vp, vp, P, P, C.c_int, Dims, vp]
     L.vbm3d_run_host.argtypes = [C.c_float, vp, vp, vp, vp, vp, P, P, C.c_int, Dims]
     L.vbm3d_gpu_similar_patches.argtypes = [P, vp, vp, vp, Dims, vp, vp, vp, vp, C.POINTER(C.c_size_t), vp]
+    L.vbm3d_gpu_bm_distance_count.argtypes = [P, vp, vp, vp, Dims, C.POINTER(C.c_ulonglong), vp]
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -159,6 +160,15 @@ def similar_patches(video, params, fflow=None, bflow=None, stream=None):
     _check(load().vbm3d_gpu_similar_patches(C.byref(params), _ptr(video), _ptr(fflow), _ptr(bflow), d, _ptr(idx),
                                             _ptr(dist), _ptr(nsimp), _ptr(nsx), None, _stream(stream)))
     return dict(idx=idx, dist=dist, nsimp=nsimp, nsx=nsx)
+
+
+def bm_distance_count(video, params, fflow=None, bflow=None, stream=None):
+    """Number of patch distances the block matching of this video evaluates."""
+    _video(video, "video")
+    n = C.c_ulonglong()
+    _check(load().vbm3d_gpu_bm_distance_count(C.byref(params), _ptr(video), _ptr(fflow), _ptr(bflow), _dims(video),
+                                              C.byref(n), _stream(stream)))
+    return n.value
 
 
 def run(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=False, stream=None):

@@ -20,7 +20,7 @@ namespace vbm3d {
 int bm_warp_bytes(const StepParams& P, int& list_cap, int& best_cap, int& win_cap);
 cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow, const float* bflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
-                      long long count, cudaStream_t stream);
+                      long long count, cudaStream_t stream, unsigned long long* out_count = nullptr);
 cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
                           const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den,
                           long long count, cudaStream_t stream);
@@ -447,6 +447,29 @@ int vbm3d_gpu_similar_patches(const vbm3d_params* prms, const float* video, cons
     CK(launch_bm(P, video, fflow, bflow, idx, distances, nsimp, ns, P.nrefs, s));
     if (!indexes) CK(cudaFreeAsync(idx, s));
     if (!nsx) CK(cudaFreeAsync(ns, s));
+    return VBM3D_OK;
+}
+
+int vbm3d_gpu_bm_distance_count(const vbm3d_params* prms, const float* video, const float* fflow,
+                                 const float* bflow, vbm3d_dims dims, unsigned long long* count, void* stream)
+{
+    if (!video || !count) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL pointer");
+    StepParams P;
+    int rc = build_params(prms, dims, 0.f, 0, P);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned *idx = nullptr, *ns = nullptr;
+    unsigned long long* d_count = nullptr;
+    CK(pool_alloc(&idx, (size_t)P.nrefs * P.N, s));
+    CK(pool_alloc(&ns, (size_t)P.nrefs, s));
+    CK(pool_alloc(&d_count, 1, s));
+    CK(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), s));
+    CK(launch_bm(P, video, fflow, bflow, idx, nullptr, nullptr, ns, P.nrefs, s, d_count));
+    CK(cudaMemcpyAsync(count, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaFreeAsync(idx, s));
+    CK(cudaFreeAsync(ns, s));
+    CK(cudaFreeAsync(d_count, s));
+    CK(cudaStreamSynchronize(s));
     return VBM3D_OK;
 }
 

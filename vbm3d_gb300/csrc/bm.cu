@@ -37,6 +37,7 @@ struct WarpBM {
     unsigned* pre;   // tempMatchesPre
     unsigned* post;  // tempMatchesPost
     int nwins;
+    int nevals;      // patchDistance evaluations so far (measurement)
 };
 
 // patchDistance for kt == 1 (src/vbm3d.cpp:965-1010).
@@ -109,6 +110,7 @@ __device__ void search_window(const StepParams& P, WarpBM& w, const float* __res
 #pragma unroll
     for (int j = 0; j < kSlots; j++) nvalid += __popc(__ballot_sync(kFull, cv[j]));
     const int m = min(P.Nb, nvalid);
+    w.nevals += nvalid;
 
     // Fast path: m rounds of warp argmin; an exact tie anywhere in the
     // selection (including at the m-th place) sends the window to the
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(128)
 bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __restrict__ fflow,
           const float* __restrict__ bflow, unsigned* __restrict__ out_idx,
           float* __restrict__ out_dist, unsigned* __restrict__ out_nsimp,
-          unsigned* __restrict__ out_nsx)
+          unsigned* __restrict__ out_nsx, unsigned long long* __restrict__ out_count)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -230,6 +232,7 @@ bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __rest
     off += 2 * kMaxNb * sizeof(unsigned);
     w.wins = reinterpret_cast<Win*>(ws + off);
     w.nwins = 0;
+    w.nevals = 0;
 
     int rx, ry, rt;
     ref_coords(P, r, rx, ry, rt);
@@ -271,6 +274,7 @@ bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __rest
         while (pw * 2 <= (unsigned)(thr + 1)) pw *= 2;
         if (out_nsimp) out_nsimp[r] = (unsigned)nsimp;
         out_nsx[r] = pw;
+        if (out_count) atomicAdd(out_count, (unsigned long long)w.nevals);
     }
 }
 
@@ -289,7 +293,7 @@ int bm_warp_bytes(const StepParams& P, int& list_cap, int& best_cap, int& win_ca
 
 cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow, const float* bflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
-                      long long count, cudaStream_t stream)
+                      long long count, cudaStream_t stream, unsigned long long* out_count)
 {
     const int warps = 4;
     const size_t smem = (size_t)warps * P.bm_warp_bytes;
@@ -299,7 +303,7 @@ cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow,
     }
     const long long blocks = (count + warps - 1) / warps;
     bm_kernel<<<(unsigned)blocks, warps * 32, smem, stream>>>(P, vid, fflow, bflow, out_idx, out_dist,
-                                                            out_nsimp, out_nsx);
+                                                            out_nsimp, out_nsx, out_count);
     return cudaGetLastError();
 }
 
