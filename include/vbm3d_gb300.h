@@ -144,6 +144,14 @@ int vbm3d_run_host(float sigma, const float *noisy, const float *fflow, const fl
                    const vbm3d_params *prms_1, const vbm3d_params *prms_2,
                    int color_space, vbm3d_dims dims);
 
+/* One step on HOST buffers (copies in, runs vbm3d_gpu_step1 or _step2,
+ * copies numerator and denominator out, waits): the call a CPU caller of
+ * vbm3d_1st_step / vbm3d_2nd_step (src/vbm3d.h:38-70) makes.  `step` is 1
+ * or 2; `basic` is read for step 2 only. */
+int vbm3d_step_host(int step, const vbm3d_params *prms, const float *noisy, const float *basic,
+                    const float *fflow, const float *bflow, vbm3d_dims dims,
+                    float sigma, int color_space, float *numerator, float *denominator);
+
 /* Block matching alone, for every reference patch of the step's grid:
  * computeSimilarPatches (src/vbm3d.cpp:1082-1197) on `video`, with the
  * reference grid of ind_initialize (src/Utilities/Utilities.cpp:400-415,

@@ -99,3 +99,20 @@ def test_invalid_dims_rejected(lib):
 def test_status_strings(lib):
     for code in range(7):
         assert lib.vbm3d_status_string(code).startswith(b"VBM3D_")
+
+
+REFERENCE_SRC = "/root/reference/src"
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_SRC), reason="reference sources not present")
+def test_dropin_shim_compiles_against_reference_headers(tmp_path):
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = ["g++", "-std=c++11", "-O1", "-w", "-c", os.path.join(root, "vbm3d_gb300", "dropin", "vbm3d_dropin.cpp"),
+           "-I", os.path.join(root, "oracle", "fftw_shim"), "-I", REFERENCE_SRC,
+           "-I", os.path.join(REFERENCE_SRC, "Utilities"), "-I", os.path.join(root, "include"),
+           "-o", str(tmp_path / "dropin.o")]
+    subprocess.check_call(cmd)
+    syms = subprocess.check_output(["nm", "-C", str(tmp_path / "dropin.o")], text=True)
+    for name in ("vbm3d_1st_step(", "vbm3d_2nd_step(", "run_vbm3d("):
+        assert any(name in line and " T " in line for line in syms.splitlines()), name

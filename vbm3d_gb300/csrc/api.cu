@@ -523,6 +523,50 @@ out:
     return rc;
 }
 
+int vbm3d_step_host(int step, const vbm3d_params* prms, const float* noisy, const float* basic,
+                    const float* fflow, const float* bflow, vbm3d_dims dims, float sigma, int color_space,
+                    float* numerator, float* denominator)
+{
+    if (step != 1 && step != 2) return fail(VBM3D_ERR_INVALID_ARGUMENT, "step must be 1 or 2, got %d", step);
+    if (!noisy || !numerator || !denominator || (step == 2 && !basic))
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL pointer");
+    StepParams P;
+    int rc = build_params(prms, dims, sigma, color_space, P);
+    if (rc) return rc;
+    const size_t n = (size_t)dims.width * dims.height * dims.frames * dims.channels;
+    const size_t nf = (size_t)dims.width * dims.height * dims.frames * 2;
+    cudaStream_t s = nullptr;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    float *d_noisy = nullptr, *d_basic = nullptr, *d_num = nullptr, *d_den = nullptr, *d_ff = nullptr,
+          *d_bf = nullptr;
+    cudaError_t e = pool_alloc(&d_noisy, n, s);
+    if (e == cudaSuccess && step == 2) e = pool_alloc(&d_basic, n, s);
+    if (e == cudaSuccess) e = pool_alloc(&d_num, n, s);
+    if (e == cudaSuccess) e = pool_alloc(&d_den, n, s);
+    if (e == cudaSuccess && fflow) e = pool_alloc(&d_ff, nf, s);
+    if (e == cudaSuccess && bflow) e = pool_alloc(&d_bf, nf, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_noisy, noisy, n * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && step == 2) e = cudaMemcpyAsync(d_basic, basic, n * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && fflow) e = cudaMemcpyAsync(d_ff, fflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && bflow) e = cudaMemcpyAsync(d_bf, bflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "device buffers");
+    } else {
+        rc = run_step(step, prms, d_noisy, d_basic, d_ff, d_bf, dims, sigma, color_space, d_num, d_den, s);
+        if (rc == VBM3D_OK) {
+            e = cudaMemcpyAsync(numerator, d_num, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(denominator, d_den, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync D2H");
+        }
+    }
+    for (float* ptr : {d_noisy, d_basic, d_num, d_den, d_ff, d_bf})
+        if (ptr) cudaFreeAsync(ptr, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess && rc == VBM3D_OK) rc = cuda_fail(e, "cudaStreamSynchronize");
+    cudaStreamDestroy(s);
+    return rc;
+}
+
 int vbm3d_run_host(float sigma, const float* noisy, const float* fflow, const float* bflow, float* basic,
                    float* denoised, const vbm3d_params* prms_1, const vbm3d_params* prms_2, int color_space,
                    vbm3d_dims dims)
