@@ -111,6 +111,26 @@ int vbm3d_gpu_step2(const vbm3d_params *prms, const float *noisy, const float *b
                     float sigma, int color_space,
                     float *numerator, float *denominator, void *stream);
 
+/* Step 1 without any device allocation.  No counterpart in the reference:
+ * it is vbm3d_gpu_step1 for callers that cannot let a library allocate
+ * device memory (plug-in hosts that own all device memory through their own
+ * allocator, real-time pipelines that forbid allocation once running,
+ * processes under a fixed memory budget).  The block-matching table that
+ * vbm3d_gpu_step1 allocates lives instead in a fixed 32 MiB device array
+ * that every GPU using this library holds until the process exits; a call
+ * needs (reference patches) * (N + 1) 4-byte words of it and returns
+ * VBM3D_ERR_UNSUPPORTED when that exceeds 8 Mi words (for 1080p RGB with
+ * the default step-1 parameters: at most 16 frames per call).  The first
+ * call on a device looks up the array's device address; make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * whose GPU work overlaps (different streams, or different host threads on
+ * one device) race: serialise them.  Same arguments and results as
+ * vbm3d_gpu_step1. */
+int vbm3d_gpu_step1_noalloc(const vbm3d_params *prms, const float *noisy,
+                            const float *fflow, const float *bflow, vbm3d_dims dims,
+                            float sigma, int color_space,
+                            float *numerator, float *denominator, void *stream);
+
 /* out[i] = denominator[i] == 0 ? fallback[i] : numerator[i] / denominator[i]
  * over `count` floats: the division in run_vbm3d (src/vbm3d.cpp:168-170,
  * :198-202).  `out` may alias `numerator`. */

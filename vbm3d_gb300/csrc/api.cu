@@ -320,6 +320,15 @@ int run_step(int step, const vbm3d_params* prms, const float* noisy, const float
 
 }  // namespace
 
+namespace vbm3d {
+// For entry points defined in other translation units.
+int build_step_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_space, StepParams& P)
+{
+    return build_params(p, d, sigma, color_space, P);
+}
+void set_last_error(int status, const char* msg) { fail(status, "%s", msg); }
+}  // namespace vbm3d
+
 extern "C" {
 
 const char* vbm3d_last_error(void) { return g_err.c_str(); }
