@@ -22,8 +22,10 @@ cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
                       long long count, cudaStream_t stream, unsigned long long* out_count = nullptr);
 cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
-                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den,
+                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den, float* pair,
                           long long count, cudaStream_t stream);
+cudaError_t launch_split_pair(const float* pair, float* num, float* den, size_t n, cudaStream_t s);
+cudaError_t launch_normalize_pair(const float* pair, const float* fb, float* out, size_t n, cudaStream_t s);
 cudaError_t launch_normalize(const float* num, const float* den, const float* fb, float* out, size_t n,
                              cudaStream_t s);
 cudaError_t launch_color(float* v, unsigned wh, unsigned frames, int forward, cudaStream_t s);
@@ -295,6 +297,23 @@ int build_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_spa
     return VBM3D_OK;
 }
 
+// One step into the interleaved (numerator, denominator) accumulator
+// `pair` (2 floats per video value), which it zeroes first.  P is validated.
+int run_step_pair(int step, const StepParams& P, const float* noisy, const float* basic, const float* fflow,
+                  const float* bflow, float* pair, cudaStream_t s)
+{
+    const size_t n = (size_t)P.whc * P.F;
+    unsigned *tab_idx = nullptr, *tab_nsx = nullptr;
+    CK(pool_alloc(&tab_idx, (size_t)P.nrefs * P.N, s));
+    CK(pool_alloc(&tab_nsx, (size_t)P.nrefs, s));
+    CK(cudaMemsetAsync(pair, 0, 2 * n * sizeof(float), s));
+    CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx, nullptr, nullptr, tab_nsx, P.nrefs, s));
+    CK(launch_filter(step, P, noisy, basic, tab_idx, tab_nsx, nullptr, nullptr, pair, P.nrefs, s));
+    CK(cudaFreeAsync(tab_idx, s));
+    CK(cudaFreeAsync(tab_nsx, s));
+    return VBM3D_OK;
+}
+
 int run_step(int step, const vbm3d_params* prms, const float* noisy, const float* basic, const float* fflow,
              const float* bflow, vbm3d_dims dims, float sigma, int color_space, float* num, float* den,
              void* stream)
@@ -306,16 +325,15 @@ int run_step(int step, const vbm3d_params* prms, const float* noisy, const float
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n = (size_t)P.whc * P.F;
-    unsigned *tab_idx = nullptr, *tab_nsx = nullptr;
-    CK(pool_alloc(&tab_idx, (size_t)P.nrefs * P.N, s));
-    CK(pool_alloc(&tab_nsx, (size_t)P.nrefs, s));
-    CK(cudaMemsetAsync(num, 0, n * sizeof(float), s));
-    CK(cudaMemsetAsync(den, 0, n * sizeof(float), s));
-    CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx, nullptr, nullptr, tab_nsx, P.nrefs, s));
-    CK(launch_filter(step, P, noisy, basic, tab_idx, tab_nsx, num, den, P.nrefs, s));
-    CK(cudaFreeAsync(tab_idx, s));
-    CK(cudaFreeAsync(tab_nsx, s));
-    return VBM3D_OK;
+    float* pair = nullptr;
+    CK(pool_alloc(&pair, 2 * n, s));
+    rc = run_step_pair(step, P, noisy, basic, fflow, bflow, pair, s);
+    if (rc == VBM3D_OK) {
+        cudaError_t e = launch_split_pair(pair, num, den, n, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "split");
+    }
+    cudaFreeAsync(pair, s);
+    return rc;
 }
 
 }  // namespace
@@ -494,6 +512,9 @@ int vbm3d_gpu_run(float sigma, float* noisy, const float* fflow, const float* bf
     if (prms_2->k > 0 && (rc = check_params(prms_2, dims))) return rc;
     float tab[3];
     if ((rc = sigma_table(sigma, dims.channels, color_space, tab))) return rc;
+    StepParams P1, P2;
+    if (prms_1->k > 0 && (rc = build_params(prms_1, dims, sigma, color_space, P1))) return rc;
+    if (prms_2->k > 0 && (rc = build_params(prms_2, dims, sigma, color_space, P2))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n = (size_t)dims.width * dims.height * dims.frames * dims.channels;
     const unsigned wh = dims.width * dims.height;
@@ -502,17 +523,23 @@ int vbm3d_gpu_run(float sigma, float* noisy, const float* fflow, const float* bf
         else rc = vbm3d_gpu_color_transform(basic, dims, 1, stream);
         if (rc) return rc;
     }
-    float *num = nullptr, *den = nullptr;
-    CK(pool_alloc(&num, n, s));
-    CK(pool_alloc(&den, n, s));
+    float* pair = nullptr;
+    CK(pool_alloc(&pair, 2 * n, s));
     if (prms_1->k > 0) {
-        if ((rc = vbm3d_gpu_step1(prms_1, noisy, fflow, bflow, dims, sigma, color_space, num, den, stream))) goto out;
-        if ((rc = vbm3d_gpu_normalize(num, den, noisy, basic, n, stream))) goto out;
+        if ((rc = run_step_pair(1, P1, noisy, nullptr, fflow, bflow, pair, s))) goto out;
+        cudaError_t e = launch_normalize_pair(pair, noisy, basic, n, s);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "normalize");
+            goto out;
+        }
     }
     if (prms_2->k > 0) {
-        if ((rc = vbm3d_gpu_step2(prms_2, noisy, basic, fflow, bflow, dims, sigma, color_space, num, den, stream)))
+        if ((rc = run_step_pair(2, P2, noisy, basic, fflow, bflow, pair, s))) goto out;
+        cudaError_t e = launch_normalize_pair(pair, basic, denoised, n, s);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "normalize");
             goto out;
-        if ((rc = vbm3d_gpu_normalize(num, den, basic, denoised, n, stream))) goto out;
+        }
     } else {
         cudaError_t e = cudaMemcpyAsync(denoised, basic, n * sizeof(float), cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) {
@@ -527,8 +554,7 @@ int vbm3d_gpu_run(float sigma, float* noisy, const float* fflow, const float* bf
         if (e != cudaSuccess) rc = cuda_fail(e, "color transform");
     }
 out:
-    cudaFreeAsync(num, s);
-    cudaFreeAsync(den, s);
+    cudaFreeAsync(pair, s);
     return rc;
 }
 

@@ -254,6 +254,26 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
+// Where the aggregation adds: separate numerator / denominator arrays (two
+// scalar reds per element), or one interleaved (numerator, denominator)
+// float2 array (one red.global.add.v2.f32 per element).
+struct AggTarget {
+    float* num;
+    float* den;
+    float* pair;
+};
+
+template <bool PAIR>
+__device__ __forceinline__ void agg_add(const AggTarget& A, size_t o, float v, float kw)
+{
+    if (PAIR) {
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(A.pair + 2 * o), "f"(v), "f"(kw) : "memory");
+    } else {
+        atomicAdd(A.num + o, v);
+        atomicAdd(A.den + o, kw);
+    }
+}
+
 // Gather the nsx patches of all channels of `vid` into slices [c][n][k*k].
 __device__ __forceinline__ void gather(const StepParams& P, const float* __restrict__ vid,
                                        const unsigned* idx, int nsx, int ss, float* g, int lane)
@@ -270,39 +290,14 @@ __device__ __forceinline__ void gather(const StepParams& P, const float* __restr
     }
 }
 
+// 1D transform along the group, shrinkage and the per-channel weights of
+// one group held in shared memory as slices [c][n][k*k] of stride ss; one
+// coefficient vector (c, pq) per lane.
 template <int STEP>
-__global__ void __launch_bounds__(128)
-filter_kernel(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
-              const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
-              float* __restrict__ num, float* __restrict__ den, int warp_floats)
+__device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* gB, int nsx, int ss, int lane,
+                                        float* wgt)
 {
-    extern __shared__ __align__(16) float fsm[];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
-    if (r >= P.nrefs) return;
-
-    const int k = P.k, k2 = k * k, C = P.C;
-    const int ss = k2 + 1;  // slice stride
-    float* base = fsm + (size_t)wid * warp_floats;
-    unsigned* idx = reinterpret_cast<unsigned*>(base);
-    float* gA = base + kMaxN;                 // noisy group (step 1: the group)
-    float* gT = gA + (size_t)C * P.N * ss;    // per-slice scratch
-    float* gB = gT + (size_t)C * P.N * ss;    // basic group (step 2)
-
-    const int nsx = (int)tab_nsx[r];
-    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
-    __syncwarp();
-
-    gather(P, noisy, idx, nsx, ss, gA, lane);
-    if (STEP == 2) gather(P, basic, idx, nsx, ss, gB, lane);
-    __syncwarp();
-    const int nsl = C * nsx;
-    for (int sl = lane; sl < nsl; sl += 32) {
-        fwd2d(gA + sl * ss, gT + sl * ss, P);
-        if (STEP == 2) fwd2d(gB + sl * ss, gT + sl * ss, P);
-    }
-    __syncwarp();
-
+    const int k2 = P.k * P.k, C = P.C;
     // 1D transform along the group + shrinkage, one (c, pq) per lane
     float acc[kMaxC] = {0.f, 0.f, 0.f};
     for (int v = lane; v < C * k2; v += 32) {
@@ -335,7 +330,6 @@ filter_kernel(const StepParams P, const float* __restrict__ noisy, const float* 
             acc[c] += ws;
         }
     }
-    float wgt[kMaxC];
 #pragma unroll
     for (int c = 0; c < kMaxC; c++) {
         const float tot = warp_sum(acc[c]);  // counts are exact; Wiener sums reassociate
@@ -344,6 +338,45 @@ filter_kernel(const StepParams P, const float* __restrict__ noisy, const float* 
         else wgt[c] = 1.f / (float)(s2 * tot);
     }
     __syncwarp();
+
+}
+
+// Any k <= 16: slices transformed in shared memory with runtime-sized loops.
+template <int STEP, bool PAIR>
+__global__ void __launch_bounds__(128)
+filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
+                      const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
+                      const AggTarget A, int warp_floats)
+{
+    extern __shared__ __align__(16) float fsm[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    if (r >= P.nrefs) return;
+
+    const int k = P.k, k2 = k * k, C = P.C;
+    const int ss = k2 + 1;  // slice stride
+    float* base = fsm + (size_t)wid * warp_floats;
+    unsigned* idx = reinterpret_cast<unsigned*>(base);
+    float* gA = base + kMaxN;                 // noisy group (step 1: the group)
+    float* gT = gA + (size_t)C * P.N * ss;    // per-slice scratch
+    float* gB = gT + (size_t)C * P.N * ss;    // basic group (step 2)
+
+    const int nsx = (int)tab_nsx[r];
+    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
+    __syncwarp();
+
+    gather(P, noisy, idx, nsx, ss, gA, lane);
+    if (STEP == 2) gather(P, basic, idx, nsx, ss, gB, lane);
+    __syncwarp();
+    const int nsl = C * nsx;
+    for (int sl = lane; sl < nsl; sl += 32) {
+        fwd2d(gA + sl * ss, gT + sl * ss, P);
+        if (STEP == 2) fwd2d(gB + sl * ss, gT + sl * ss, P);
+    }
+    __syncwarp();
+
+    float wgt[kMaxC];
+    group_1d<STEP>(P, gA, gB, nsx, ss, lane, wgt);
 
     float* ge = STEP == 1 ? gA : gB;
     for (int sl = lane; sl < nsl; sl += 32) inv2d(ge + sl * ss, gT + sl * ss, P);
@@ -359,39 +392,245 @@ filter_kernel(const StepParams P, const float* __restrict__ noisy, const float* 
         patch_coords(P, idx[n], x, y, t);
         const size_t o = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)(y + p) * P.W + x + q;
         const float kw = P.kaiser[pq] * wgt[c];
-        atomicAdd(num + o, kw * ge[sl * ss + pq]);
-        atomicAdd(den + o, kw);
+        agg_add<PAIR>(A, o, kw * ge[sl * ss + pq], kw);
     }
 }
 
-int filter_warp_floats(const StepParams& P, int step)
+// ------------------------------------------------- register-resident ---
+// One slice per lane for compile-time K: the k x k block lives in
+// registers, loops are unrolled so every table entry is a constant-bank
+// operand of the FMA/MUL that uses it.
+
+template <int K>
+__device__ __forceinline__ void reg_fwd2d(float* x, const StepParams& P)
 {
-    const int ss = P.k * P.k + 1;
-    const int groups = step == 1 ? 2 : 3;  // group(s) + scratch
-    return kMaxN + groups * P.C * P.N * ss;
+    float t[K * K];
+    if (K == 8 && P.T2D == kBIOR) {
+        // bior_2d_forward (src/lib_transforms.cpp:158-176), float order kept
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; q++) m = m + x[i * K + q] * P.fwd[j * K + q];
+                t[i * K + j] = m;
+            }
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; q++) m = m + t[q * K + i] * P.fwd[j * K + q];
+                x[i * K + j] = m;
+            }
+    } else {
+        // REDFT10 along rows then columns, then coef_norm (src/vbm3d.cpp:1294-1302)
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int v = 0; v < K; v++) {
+                float m = 0.f;
+#pragma unroll
+                for (int j = 0; j < K; j++) m = __fmaf_rn(x[i * K + j], P.fwd[v * K + j], m);
+                t[i * K + v] = m;
+            }
+#pragma unroll
+        for (int u = 0; u < K; u++)
+#pragma unroll
+            for (int v = 0; v < K; v++) {
+                float m = 0.f;
+#pragma unroll
+                for (int i = 0; i < K; i++) m = __fmaf_rn(P.fwd[u * K + i], t[i * K + v], m);
+                x[u * K + v] = m * P.cn[u * K + v];
+            }
+    }
 }
 
-cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
-                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den,
-                          long long count, cudaStream_t stream)
+template <int K>
+__device__ __forceinline__ void reg_inv2d(float* x, const StepParams& P)
+{
+    float t[K * K];
+    if (K == 8 && P.T2D == kBIOR) {
+        // bior_2d_inverse (src/lib_transforms.cpp:294-320)
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; q++) m = m + x[i + q * K] * P.inv[j * K + q];
+                t[i * K + j] = m;
+            }
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; q++) m = m + t[q * K + i] * P.inv[j * K + q];
+                x[j * K + i] = m;
+            }
+    } else {
+        // dct_2d_inv (src/vbm3d.cpp:1696-1709)
+#pragma unroll
+        for (int e = 0; e < K * K; e++) x[e] = x[e] * P.cni[e];
+#pragma unroll
+        for (int u = 0; u < K; u++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int v = 0; v < K; v++) m = __fmaf_rn(x[u * K + v], P.inv[j * K + v], m);
+                t[u * K + j] = m;
+            }
+        const float coef = 1.0f / (float)(K * 2);
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                float m = 0.f;
+#pragma unroll
+                for (int u = 0; u < K; u++) m = __fmaf_rn(P.inv[i * K + u], t[u * K + j], m);
+                x[i * K + j] = coef * m;
+            }
+    }
+}
+
+template <int STEP, int K, bool PAIR>
+__global__ void __launch_bounds__(128)
+filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
+                const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx, const AggTarget A,
+                int warp_floats)
+{
+    constexpr int K2 = K * K, SS = K2 + 1;
+    extern __shared__ __align__(16) float fsm[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    if (r >= P.nrefs) return;
+
+    const int C = P.C;
+    float* base = fsm + (size_t)wid * warp_floats;
+    unsigned* idx = reinterpret_cast<unsigned*>(base);
+    float* gA = base + kMaxN;               // noisy group coefficients
+    float* gB = gA + (size_t)C * P.N * SS;  // basic group coefficients (step 2)
+
+    const int nsx = (int)tab_nsx[r];
+    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
+    __syncwarp();
+    const int nsl = C * nsx;
+
+    // 2D transforms, one slice (c, n) per lane
+    for (int sl = lane; sl < nsl; sl += 32) {
+        const int c = sl / nsx, n = sl - c * nsx;
+        int x, y, t;
+        patch_coords(P, idx[n], x, y, t);
+        const size_t off = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)y * P.W + x;
+        float v[K2];
+#pragma unroll
+        for (int p = 0; p < K; p++)
+#pragma unroll
+            for (int q = 0; q < K; q++) v[p * K + q] = __ldg(noisy + off + (size_t)p * P.W + q);
+        reg_fwd2d<K>(v, P);
+#pragma unroll
+        for (int e = 0; e < K2; e++) gA[sl * SS + e] = v[e];
+        if (STEP == 2) {
+#pragma unroll
+            for (int p = 0; p < K; p++)
+#pragma unroll
+                for (int q = 0; q < K; q++) v[p * K + q] = __ldg(basic + off + (size_t)p * P.W + q);
+            reg_fwd2d<K>(v, P);
+#pragma unroll
+            for (int e = 0; e < K2; e++) gB[sl * SS + e] = v[e];
+        }
+    }
+    __syncwarp();
+
+    float wgt[kMaxC];
+    group_1d<STEP>(P, gA, gB, nsx, SS, lane, wgt);
+
+    // inverse 2D + aggregation (src/vbm3d.cpp:612-650), one slice per lane
+    const float* ge = STEP == 1 ? gA : gB;
+    for (int sl = lane; sl < nsl; sl += 32) {
+        const int c = sl / nsx, n = sl - c * nsx;
+        float v[K2];
+#pragma unroll
+        for (int e = 0; e < K2; e++) v[e] = ge[sl * SS + e];
+        reg_inv2d<K>(v, P);
+        int x, y, t;
+        patch_coords(P, idx[n], x, y, t);
+        const size_t off = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)y * P.W + x;
+        const float w = wgt[c];
+#pragma unroll
+        for (int p = 0; p < K; p++)
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const float kw = P.kaiser[p * K + q] * w;
+                agg_add<PAIR>(A, off + (size_t)p * P.W + q, kw * v[p * K + q], kw);
+            }
+    }
+}
+
+namespace {
+
+template <int STEP, int K, bool PAIR>
+cudaError_t launch_k(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                     const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
 {
     const int warps = 4;
-    const int wf = filter_warp_floats(P, step);
+    const int wf = kMaxN + (STEP == 1 ? 1 : 2) * P.C * P.N * (K * K + 1);
     const size_t smem = (size_t)warps * wf * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     const long long blocks = (count + warps - 1) / warps;
-    cudaError_t e;
-    if (step == 1) {
-        e = cudaFuncSetAttribute(filter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        filter_kernel<1><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx, tab_nsx, num,
-                                                                        den, wf);
-    } else {
-        e = cudaFuncSetAttribute(filter_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        filter_kernel<2><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx, tab_nsx, num,
-                                                                        den, wf);
-    }
+    filter_kernel_k<STEP, K, PAIR><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
+                                                                                  tab_nsx, A, wf);
     return cudaGetLastError();
+}
+
+template <int STEP, bool PAIR>
+cudaError_t launch_generic(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                           const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+{
+    const int warps = 4;
+    const int wf = kMaxN + (STEP == 1 ? 2 : 3) * P.C * P.N * (P.k * P.k + 1);  // group(s) + scratch
+    const size_t smem = (size_t)warps * wf * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(filter_kernel_generic<STEP, PAIR>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long blocks = (count + warps - 1) / warps;
+    filter_kernel_generic<STEP, PAIR><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
+                                                                                     tab_nsx, A, wf);
+    return cudaGetLastError();
+}
+
+template <int STEP, bool PAIR>
+cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                     const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+{
+    switch (P.k) {
+        case 7: return launch_k<STEP, 7, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+        case 8: return launch_k<STEP, 8, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+        default: return launch_generic<STEP, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    }
+}
+
+}  // namespace
+
+// Aggregates into num / den when `pair` is NULL, else into the interleaved
+// (num, den) array `pair` (2 floats per video value).
+cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
+                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den, float* pair,
+                          long long count, cudaStream_t stream)
+{
+    const AggTarget A{num, den, pair};
+    if (step == 1)
+        return pair ? dispatch<1, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
+                    : dispatch<1, false>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    return pair ? dispatch<2, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
+                : dispatch<2, false>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
 }
 
 }  // namespace vbm3d

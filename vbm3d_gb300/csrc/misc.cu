@@ -32,6 +32,27 @@ __global__ void normalize_kernel(const float* num, const float* __restrict__ den
     }
 }
 
+// Interleaved (num, den) accumulator -> separate numerator / denominator.
+__global__ void split_pair_kernel(const float2* __restrict__ pair, float* __restrict__ num, float* __restrict__ den,
+                                  size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = pair[i];
+        num[i] = v.x;
+        den[i] = v.y;
+    }
+}
+
+// run_vbm3d's division read straight from the interleaved accumulator.
+__global__ void normalize_pair_kernel(const float2* __restrict__ pair, const float* __restrict__ fb,
+                                      float* __restrict__ out, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = pair[i];
+        out[i] = v.y == 0 ? fb[i] : v.x / v.y;
+    }
+}
+
 // transformColorSpace, 3 channels (src/Utilities/LibVideoT.hpp:763-888);
 // float operations in the reference's order.
 __global__ void color_kernel(float* __restrict__ v, unsigned wh, unsigned frames, int forward)
@@ -73,6 +94,18 @@ cudaError_t launch_normalize(const float* num, const float* den, const float* fb
                              cudaStream_t s)
 {
     normalize_kernel<<<grid_for(n / 4 + 1, 256), 256, 0, s>>>(num, den, fb, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_pair(const float* pair, float* num, float* den, size_t n, cudaStream_t s)
+{
+    split_pair_kernel<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const float2*>(pair), num, den, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_normalize_pair(const float* pair, const float* fb, float* out, size_t n, cudaStream_t s)
+{
+    normalize_pair_kernel<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const float2*>(pair), fb, out, n);
     return cudaGetLastError();
 }
 
