@@ -291,10 +291,19 @@ int bm_warp_bytes(const StepParams& P, int& list_cap, int& best_cap, int& win_ca
     return (int)((off + 15) & ~size_t(15));
 }
 
+bool bm2_supported(const StepParams& P);
+cudaError_t launch_bm2(const StepParams& P, const float* vid, const float* fflow, const float* bflow,
+                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx, long long count,
+                       cudaStream_t stream);
+
+// The staged kernel (bm2.cu) for the shapes it handles, this one otherwise
+// and whenever the distance count is requested.
 cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow, const float* bflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
                       long long count, cudaStream_t stream, unsigned long long* out_count)
 {
+    if (!out_count && bm2_supported(P))
+        return launch_bm2(P, vid, fflow, bflow, out_idx, out_dist, out_nsimp, out_nsx, count, stream);
     const int warps = 4;
     const size_t smem = (size_t)warps * P.bm_warp_bytes;
     if (smem > 48 * 1024) {
