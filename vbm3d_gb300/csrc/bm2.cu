@@ -39,6 +39,21 @@ struct PWin {
 
 static_assert(sizeof(PWin) % 16 == 0, "phase windows stay 8-byte aligned in shared memory");
 
+// Inside the kernel a patch is named by packed coordinates
+// ((t - rt + 32) << 26) | (y << 13) | x (x, y < 8192, |t - rt| <= 16),
+// which decode without divisions; the output converts them to the
+// reference's linear indices.
+__device__ __forceinline__ unsigned pack_xyt(int x, int y, int t, int rt)
+{
+    return ((unsigned)(t - rt + 32) << 26) | ((unsigned)y << 13) | (unsigned)x;
+}
+__device__ __forceinline__ void unpack_xyt(unsigned v, int rt, int& x, int& y, int& t)
+{
+    x = (int)(v & 8191u);
+    y = (int)((v >> 13) & 8191u);
+    t = (int)(v >> 26) - 32 + rt;
+}
+
 // Row of position j in a window of width ww (exact: j < 2^8, ww <= 15).
 __device__ __forceinline__ int pos_row(int j, float rcp_ww) { return (int)(((float)j + 0.5f) * rcp_ww); }
 
@@ -201,7 +216,7 @@ __device__ void small_partial_sort(Pair* a, int m, int n, int lane)
 }
 
 template <int K, int C>
-__device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int lane, int rx, int ry,
+__device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
                                 int pitch, int plane)
 {
     constexpr int KK = K * K;
@@ -266,7 +281,7 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
             if (two) {
                 const float* t2 = tp[2] + c * plane;
                 const float* t3 = tp[3] + c * plane;
-#pragma unroll
+#pragma unroll 1
                 for (int hy = 0; hy < K; hy++)
 #pragma unroll
                     for (int hx = 0; hx < K; hx++) {
@@ -275,7 +290,7 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
                         sq_acc2(a1x, a1y, r2.x, r2.y, t2[hy * pitch + hx], t3[hy * pitch + hx]);
                     }
             } else {
-#pragma unroll
+#pragma unroll 1
                 for (int hy = 0; hy < K; hy++)
 #pragma unroll
                     for (int hx = 0; hx < K; hx++) {
@@ -310,7 +325,7 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
                 float d = acc[q] / norm;
                 if (qx == rx && qy == ry) d = d - P.dbias;
                 e.d = d;
-                e.i = patch_index(P, qx, qy, pwn.t);
+                e.i = pack_xyt(qx, qy, pwn.t, rt);
             }
             S.res[rslot[q]] = e;
         }
@@ -320,34 +335,36 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
 
 // Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
 // channels, at tile pitch `pitch`.
+// 4-byte asynchronous global -> shared copy (no register round trip).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+
 template <int K, int C>
 __device__ void stage_tiles(const StepParams& P, const Smem& S, const float* __restrict__ vid, int nw, int lane,
                             int pitch, int plane)
 {
+    // every tile row of every window is copied asynchronously, then waited
+    // for once: the loads of the whole phase are in flight together
     for (int w = 0; w < nw; w++) {
         const PWin pwn = S.pw[w];
         const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
         const float* src = vid + (size_t)pwn.t * P.whc + (size_t)pwn.y0 * P.W + pwn.x0;
         float* dst = S.tiles + pwn.tile;
-        if (tw <= 16) {
-            // two rows per pass, 16 lanes per row
-            const int x = lane & 15, y0 = lane >> 4;
-            if (x < tw) {
+        const int x = tw <= 16 ? (lane & 15) : lane, ystep = tw <= 16 ? 2 : 1, y0 = tw <= 16 ? (lane >> 4) : 0;
+        if (x < tw) {
 #pragma unroll 1
-                for (int c = 0; c < C; c++) {
-                    const float* sc = src + (size_t)c * P.wh;
-                    float* dc = dst + c * plane;
+            for (int c = 0; c < C; c++) {
+                const float* sc = src + (size_t)c * P.wh + x;
+                float* dc = dst + c * plane + x;
 #pragma unroll 4
-                    for (int y = y0; y < th; y += 2) dc[y * pitch + x] = __ldg(sc + (size_t)y * P.W + x);
-                }
+                for (int y = y0; y < th; y += ystep) cp_async4(dc + y * pitch, sc + (size_t)y * P.W);
             }
-        } else if (lane < tw) {
-#pragma unroll 1
-            for (int c = 0; c < C; c++)
-#pragma unroll 4
-                for (int y = 0; y < th; y++) dst[c * plane + y * pitch + lane] = __ldg(src + (size_t)c * P.wh + (size_t)y * P.W + lane);
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncwarp();
 }
 
@@ -443,7 +460,7 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
         }
         __syncwarp();
         stage_tiles<K, C>(P, S, vid, 1, lane, pitch, plane);
-        phase_distances<K, C>(P, S, 1, lane, rx, ry, pitch, plane);
+        phase_distances<K, C>(P, S, 1, lane, rx, ry, rt, pitch, plane);
         register_windows(S, 1, lane);
         int n0 = 0;
         select_window(P, S, S.pw[0], lane, S.best, n0, S.scr);
@@ -465,36 +482,43 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
     const int pitch = bm2_pitch(P.Npr, K), plane = pitch * (P.Npr + K - 1);
     const int tile_sz = C * plane;
     for (int f = 1; f <= nphase; f++) {
-        // windows of this phase: forward step f (src/vbm3d.cpp:1126-1133),
-        // then backward step f (:1150-1157)
-        int nw = 0;
-        if (lane == 0) {
-            int res = 0;
-            for (int chain = 1; chain <= 2; chain++) {
-                if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
+        // windows of this phase, one per lane: forward step f
+        // (src/vbm3d.cpp:1126-1133), then backward step f (:1150-1157)
+        const bool fa = f <= fend, ba = f <= bend;
+        const int nw = (fa ? Nb : 0) + (ba ? Nb : 0);
+        {
+            PWin w;
+            int n = 0;
+            if (lane < nw) {
+                const int chain = (fa && lane < Nb) ? 1 : 2;
+                const int m = chain == 1 ? lane : lane - (fa ? Nb : 0);
+                int px, py, pt;
+                unpack_xyt(S.cen[(chain - 1) * kMaxNb + m], rt, px, py, pt);
                 const float* flow = chain == 1 ? fflow : bflow;
-                for (int m = 0; m < Nb; m++) {
-                    int px, py, pt;
-                    patch_coords(P, S.cen[(chain - 1) * kMaxNb + m], px, py, pt);
-                    const int ft = chain == 1 ? pt : pt - 1;
-                    const float* fl = flow ? flow + (size_t)ft * 2 * P.wh : nullptr;
-                    const float fx = fl ? __ldg(fl + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
-                    px = min(max((int)((float)px + roundf(fx)), 0), P.W - K);
-                    const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
-                    py = min(max((int)((float)py + roundf(fy)), 0), P.H - K);
-                    PWin w = make_window(P, chain == 1 ? pt + 1 : pt - 1, px, py, P.Npr, chain);
-                    w.tile = nw * tile_sz;
-                    w.res = res;
-                    res += npos(w);
-                    S.pw[nw] = w;
-                    S.cnt[3 + nw] = S.cnt[2] + nw;  // earlier windows: all registered + earlier in this phase
-                    nw++;
-                }
+                const int ft = chain == 1 ? pt : pt - 1;  // fflow(.., pt) / bflow(.., pt - 1)
+                const float* fl = flow ? flow + (size_t)ft * 2 * P.wh : nullptr;
+                const float fx = fl ? __ldg(fl + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
+                px = min(max((int)((float)px + roundf(fx)), 0), P.W - K);
+                const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
+                py = min(max((int)((float)py + roundf(fy)), 0), P.H - K);
+                w = make_window(P, chain == 1 ? pt + 1 : pt - 1, px, py, P.Npr, chain);
+                w.tile = lane * tile_sz;
+                n = npos(w);
             }
-            S.cnt[0] = nw;
+            // exclusive prefix sum of the window sizes: result offsets
+            int incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane < nw) {
+                w.res = incl - n;
+                S.pw[lane] = w;
+                S.cnt[3 + lane] = S.cnt[2] + lane;  // earlier windows: all registered + earlier in this phase
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        nw = S.cnt[0];
         // this phase's windows must be visible to the seen test of later
         // windows of the same phase: register them first, then test each
         // window against the windows registered before it (S.cnt[3 + w])
@@ -508,7 +532,7 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
         }
         __syncwarp();
         stage_tiles<K, C>(P, S, vid, nw, lane, pitch, plane);
-        phase_distances<K, C>(P, S, nw, lane, rx, ry, pitch, plane);
+        phase_distances<K, C>(P, S, nw, lane, rx, ry, rt, pitch, plane);
 
         // per chain: top-Nb of each window, then of their union
         int w0 = 0;
@@ -549,7 +573,13 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
     else if (lane == 0) partial_sort(lst, nsimp, nbest);
     __syncwarp();
     if (lane < P.N) {
-        out_idx[(size_t)r * P.N + lane] = lane < nsimp ? lst[lane].i : kNone;
+        unsigned oi = kNone;
+        if (lane < nsimp) {
+            int x, y, t;
+            unpack_xyt(lst[lane].i, rt, x, y, t);
+            oi = patch_index(P, x, y, t);
+        }
+        out_idx[(size_t)r * P.N + lane] = oi;
         if (out_dist) out_dist[(size_t)r * P.N + lane] = lane < nsimp ? lst[lane].d : 0.f;
     }
     if (lane == 0) {
@@ -569,7 +599,9 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
 Layout bm2_layout(const StepParams& P)
 {
     Layout L{0, 0, 0, 0};
-    if (!((P.k == 7 || P.k == 8) && (P.C == 1 || P.C == 3) && P.kt == 1 && P.bm_win_cap <= 64)) return L;
+    if (!((P.k == 7 || P.k == 8) && (P.C == 1 || P.C == 3) && P.kt == 1 && P.bm_win_cap <= 64 && P.W <= 8192 &&
+          P.H <= 8192 && P.Nf <= 16))
+        return L;
     const int p0 = bm2_pitch(P.Ns, P.k), p1 = bm2_pitch(P.Npr, P.k);
     L.tile_floats = max(P.C * p0 * (P.Ns + P.k - 1), 2 * P.Nb * P.C * p1 * (P.Npr + P.k - 1));
     L.tile_floats = (L.tile_floats + 3) & ~3;
