@@ -293,7 +293,7 @@ __device__ __forceinline__ void gather(const StepParams& P, const float* __restr
 // 1D transform along the group, shrinkage and the per-channel weights of
 // one group held in shared memory as slices [c][n][k*k] of stride ss; one
 // coefficient vector (c, pq) per lane.
-template <int STEP>
+template <int STEP, int NMAX = 32>
 __device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* gB, int nsx, int ss, int lane,
                                         float* wgt)
 {
@@ -311,9 +311,9 @@ __device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* 
                 case 1: kept = ht_vector<1>(ga, ss, pq == 0, T, P.T3D); break;
                 case 2: kept = ht_vector<2>(ga, ss, pq == 0, T, P.T3D); break;
                 case 4: kept = ht_vector<4>(ga, ss, pq == 0, T, P.T3D); break;
-                case 8: kept = ht_vector<8>(ga, ss, pq == 0, T, P.T3D); break;
-                case 16: kept = ht_vector<16>(ga, ss, pq == 0, T, P.T3D); break;
-                default: kept = ht_vector<32>(ga, ss, pq == 0, T, P.T3D); break;
+                case 8: kept = ht_vector<(NMAX < 8 ? NMAX : 8)>(ga, ss, pq == 0, T, P.T3D); break;
+                case 16: kept = ht_vector<(NMAX < 16 ? NMAX : 16)>(ga, ss, pq == 0, T, P.T3D); break;
+                default: kept = ht_vector<NMAX>(ga, ss, pq == 0, T, P.T3D); break;
             }
             acc[c] += (float)kept;
         } else {
@@ -323,9 +323,9 @@ __device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* 
                 case 1: ws = wiener_vector<1>(ga, gb, ss, s2, P.T3D); break;
                 case 2: ws = wiener_vector<2>(ga, gb, ss, s2, P.T3D); break;
                 case 4: ws = wiener_vector<4>(ga, gb, ss, s2, P.T3D); break;
-                case 8: ws = wiener_vector<8>(ga, gb, ss, s2, P.T3D); break;
-                case 16: ws = wiener_vector<16>(ga, gb, ss, s2, P.T3D); break;
-                default: ws = wiener_vector<32>(ga, gb, ss, s2, P.T3D); break;
+                case 8: ws = wiener_vector<(NMAX < 8 ? NMAX : 8)>(ga, gb, ss, s2, P.T3D); break;
+                case 16: ws = wiener_vector<(NMAX < 16 ? NMAX : 16)>(ga, gb, ss, s2, P.T3D); break;
+                default: ws = wiener_vector<NMAX>(ga, gb, ss, s2, P.T3D); break;
             }
             acc[c] += ws;
         }
@@ -401,105 +401,126 @@ filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const
 // registers, loops are unrolled so every table entry is a constant-bank
 // operand of the FMA/MUL that uses it.
 
-template <int K>
-__device__ __forceinline__ void reg_fwd2d(float* x, const StepParams& P)
+// In-place passes over a K x K block held in registers, K temporaries.
+// row_pass: x[i][v] = sum_j x[i][j] M[v][j]; col_pass: x[u][j] = sum_i
+// M[u][i] x[i][j]; sums run from index 0 upwards.  EXACT selects separate
+// multiply and add roundings (the reference's float loops); otherwise FMA.
+template <int K, bool EXACT>
+__device__ __forceinline__ void row_pass(float* x, const float* M)
 {
-    float t[K * K];
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        float y[K];
+#pragma unroll
+        for (int v = 0; v < K; v++) {
+            float m = 0.f;
+#pragma unroll
+            for (int j = 0; j < K; j++) m = EXACT ? m + x[i * K + j] * M[v * K + j] : __fmaf_rn(x[i * K + j], M[v * K + j], m);
+            y[v] = m;
+        }
+#pragma unroll
+        for (int v = 0; v < K; v++) x[i * K + v] = y[v];
+    }
+}
+
+template <int K, bool EXACT>
+__device__ __forceinline__ void col_pass(float* x, const float* M)
+{
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        float y[K];
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            float m = 0.f;
+#pragma unroll
+            for (int i = 0; i < K; i++) m = EXACT ? m + x[i * K + j] * M[u * K + i] : __fmaf_rn(M[u * K + i], x[i * K + j], m);
+            y[u] = m;
+        }
+#pragma unroll
+        for (int u = 0; u < K; u++) x[u * K + j] = y[u];
+    }
+}
+
+// Forward 2D transform of slice g (stride-1 K*K floats in shared memory),
+// through registers, result back in g.
+template <int K>
+__device__ __forceinline__ void slice_fwd2d(float* g, const StepParams& P)
+{
+    float x[K * K];
+#pragma unroll
+    for (int e = 0; e < K * K; e++) x[e] = g[e];
     if (K == 8 && P.T2D == kBIOR) {
-        // bior_2d_forward (src/lib_transforms.cpp:158-176), float order kept
+        // bior_2d_forward (src/lib_transforms.cpp:158-176): t = X B^T (rows),
+        // out[i][j] = sum_q t[q][i] B[j][q], i.e. the column pass gives out^T
+        row_pass<K, true>(x, P.fwd);
+        col_pass<K, true>(x, P.fwd);
 #pragma unroll
         for (int i = 0; i < K; i++)
 #pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; q++) m = m + x[i * K + q] * P.fwd[j * K + q];
-                t[i * K + j] = m;
-            }
-#pragma unroll
-        for (int i = 0; i < K; i++)
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; q++) m = m + t[q * K + i] * P.fwd[j * K + q];
-                x[i * K + j] = m;
-            }
+            for (int j = 0; j < K; j++) g[i * K + j] = x[j * K + i];
     } else {
         // REDFT10 along rows then columns, then coef_norm (src/vbm3d.cpp:1294-1302)
+        row_pass<K, false>(x, P.fwd);
+        col_pass<K, false>(x, P.fwd);
 #pragma unroll
-        for (int i = 0; i < K; i++)
-#pragma unroll
-            for (int v = 0; v < K; v++) {
-                float m = 0.f;
-#pragma unroll
-                for (int j = 0; j < K; j++) m = __fmaf_rn(x[i * K + j], P.fwd[v * K + j], m);
-                t[i * K + v] = m;
-            }
-#pragma unroll
-        for (int u = 0; u < K; u++)
-#pragma unroll
-            for (int v = 0; v < K; v++) {
-                float m = 0.f;
-#pragma unroll
-                for (int i = 0; i < K; i++) m = __fmaf_rn(P.fwd[u * K + i], t[i * K + v], m);
-                x[u * K + v] = m * P.cn[u * K + v];
-            }
+        for (int e = 0; e < K * K; e++) g[e] = x[e] * P.cn[e];
     }
 }
 
 template <int K>
-__device__ __forceinline__ void reg_inv2d(float* x, const StepParams& P)
+__device__ __forceinline__ void slice_inv2d(float* g, const StepParams& P)
 {
-    float t[K * K];
+    float x[K * K];
+#pragma unroll
+    for (int e = 0; e < K * K; e++) x[e] = g[e];
     if (K == 8 && P.T2D == kBIOR) {
-        // bior_2d_inverse (src/lib_transforms.cpp:294-320)
+        // bior_2d_inverse (src/lib_transforms.cpp:294-320): temp = in^T;
+        // t2 = temp B^T, computed as a column pass on `in` (gives t2^T);
+        // then the row pass gives temp[i][j]; signal[j][i] = temp[i][j]
+        col_pass<K, true>(x, P.inv);
+        row_pass<K, true>(x, P.inv);
 #pragma unroll
         for (int i = 0; i < K; i++)
 #pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; q++) m = m + x[i + q * K] * P.inv[j * K + q];
-                t[i * K + j] = m;
-            }
-#pragma unroll
-        for (int i = 0; i < K; i++)
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; q++) m = m + t[q * K + i] * P.inv[j * K + q];
-                x[j * K + i] = m;
-            }
+            for (int j = 0; j < K; j++) g[j * K + i] = x[i * K + j];
     } else {
         // dct_2d_inv (src/vbm3d.cpp:1696-1709)
 #pragma unroll
         for (int e = 0; e < K * K; e++) x[e] = x[e] * P.cni[e];
-#pragma unroll
-        for (int u = 0; u < K; u++)
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int v = 0; v < K; v++) m = __fmaf_rn(x[u * K + v], P.inv[j * K + v], m);
-                t[u * K + j] = m;
-            }
+        row_pass<K, false>(x, P.inv);
+        col_pass<K, false>(x, P.inv);
         const float coef = 1.0f / (float)(K * 2);
 #pragma unroll
-        for (int i = 0; i < K; i++)
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                float m = 0.f;
-#pragma unroll
-                for (int u = 0; u < K; u++) m = __fmaf_rn(P.inv[i * K + u], t[u * K + j], m);
-                x[i * K + j] = coef * m;
-            }
+        for (int e = 0; e < K * K; e++) g[e] = coef * x[e];
     }
 }
 
+// Gathers the nsx patches of every channel into slices [c][n][K*K] of
+// stride SS, lanes over consecutive pixels (each patch row is contiguous in
+// memory, so a warp load touches a few rows instead of 32 patches).  idx[n]
+// is the patch's linear index in channel 0; log2n = log2(nsx).
+template <int K, int SS>
+__device__ __forceinline__ void gather_k(const StepParams& P, const float* __restrict__ vid, const unsigned* idx,
+                                         int nsx, int log2n, float* g, int lane)
+{
+    constexpr int K2 = K * K;
+    const int total = P.C * nsx * K2;
+    for (int e = lane; e < total; e += 32) {
+        const int sl = e / K2, pq = e - sl * K2;
+        const int c = sl >> log2n, n = sl & (nsx - 1);
+        const int p = pq / K, q = pq - p * K;
+        g[sl * SS + pq] = __ldg(vid + idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q);
+    }
+}
+
+template <int K, int SS>
+__device__ __forceinline__ void slice_fwd(const StepParams& P, float* g, int nsl, int lane)
+{
+    for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(g + sl * SS, P);
+}
+
 template <int STEP, int K, bool PAIR>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 4)
 filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
                 const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx, const AggTarget A,
                 int warp_floats)
@@ -513,62 +534,39 @@ filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float
     const int C = P.C;
     float* base = fsm + (size_t)wid * warp_floats;
     unsigned* idx = reinterpret_cast<unsigned*>(base);
-    float* gA = base + kMaxN;               // noisy group coefficients
-    float* gB = gA + (size_t)C * P.N * SS;  // basic group coefficients (step 2)
+    float* gA = base + kMaxN;               // noisy group
+    float* gB = gA + (size_t)C * P.N * SS;  // basic group (step 2)
 
     const int nsx = (int)tab_nsx[r];
+    const int log2n = __ffs(nsx) - 1;
     if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
     __syncwarp();
     const int nsl = C * nsx;
 
-    // 2D transforms, one slice (c, n) per lane
-    for (int sl = lane; sl < nsl; sl += 32) {
-        const int c = sl / nsx, n = sl - c * nsx;
-        int x, y, t;
-        patch_coords(P, idx[n], x, y, t);
-        const size_t off = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)y * P.W + x;
-        float v[K2];
-#pragma unroll
-        for (int p = 0; p < K; p++)
-#pragma unroll
-            for (int q = 0; q < K; q++) v[p * K + q] = __ldg(noisy + off + (size_t)p * P.W + q);
-        reg_fwd2d<K>(v, P);
-#pragma unroll
-        for (int e = 0; e < K2; e++) gA[sl * SS + e] = v[e];
-        if (STEP == 2) {
-#pragma unroll
-            for (int p = 0; p < K; p++)
-#pragma unroll
-                for (int q = 0; q < K; q++) v[p * K + q] = __ldg(basic + off + (size_t)p * P.W + q);
-            reg_fwd2d<K>(v, P);
-#pragma unroll
-            for (int e = 0; e < K2; e++) gB[sl * SS + e] = v[e];
-        }
-    }
+    gather_k<K, SS>(P, noisy, idx, nsx, log2n, gA, lane);
+    if (STEP == 2) gather_k<K, SS>(P, basic, idx, nsx, log2n, gB, lane);
+    __syncwarp();
+    // 2D transforms, one slice (c, n) per lane, in registers
+    slice_fwd<K, SS>(P, gA, nsl, lane);
+    if (STEP == 2) slice_fwd<K, SS>(P, gB, nsl, lane);
     __syncwarp();
 
     float wgt[kMaxC];
-    group_1d<STEP>(P, gA, gB, nsx, SS, lane, wgt);
+    group_1d<STEP, 8>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
 
-    // inverse 2D + aggregation (src/vbm3d.cpp:612-650), one slice per lane
-    const float* ge = STEP == 1 ? gA : gB;
-    for (int sl = lane; sl < nsl; sl += 32) {
-        const int c = sl / nsx, n = sl - c * nsx;
-        float v[K2];
-#pragma unroll
-        for (int e = 0; e < K2; e++) v[e] = ge[sl * SS + e];
-        reg_inv2d<K>(v, P);
-        int x, y, t;
-        patch_coords(P, idx[n], x, y, t);
-        const size_t off = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)y * P.W + x;
-        const float w = wgt[c];
-#pragma unroll
-        for (int p = 0; p < K; p++)
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const float kw = P.kaiser[p * K + q] * w;
-                agg_add<PAIR>(A, off + (size_t)p * P.W + q, kw * v[p * K + q], kw);
-            }
+    // inverse 2D, one slice per lane
+    float* ge = STEP == 1 ? gA : gB;
+    for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(ge + sl * SS, P);
+    __syncwarp();
+
+    // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
+    const int total = nsl * K2;
+    for (int e = lane; e < total; e += 32) {
+        const int sl = e / K2, pq = e - sl * K2;
+        const int c = sl >> log2n, n = sl & (nsx - 1);
+        const int p = pq / K, q = pq - p * K;
+        const float kw = P.kaiser[pq] * wgt[c];
+        agg_add<PAIR>(A, idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q, kw * ge[sl * SS + pq], kw);
     }
 }
 
@@ -610,11 +608,14 @@ template <int STEP, bool PAIR>
 cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
                      const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
 {
-    switch (P.k) {
-        case 7: return launch_k<STEP, 7, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
-        case 8: return launch_k<STEP, 8, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
-        default: return launch_generic<STEP, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    if (P.N <= 8) {  // group sizes up to 8: the register-resident kernel
+        switch (P.k) {
+            case 7: return launch_k<STEP, 7, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+            case 8: return launch_k<STEP, 8, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+            default: break;
+        }
     }
+    return launch_generic<STEP, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
 }
 
 }  // namespace
