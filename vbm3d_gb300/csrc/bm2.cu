@@ -220,33 +220,37 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
                                 int pitch, int plane)
 {
     constexpr int KK = K * K;
-    // pair windows (0,1), (2,3), ...; an odd last window is split in halves
+    // pair windows (0,1), (2,3), ...; an odd last window is split in
+    // halves.  Each pair owns whole 32-lane rows of slots (slot j of a pair
+    // = position j of both windows), so one load instruction reads one tile
+    // and the rows of a window fall on distinct banks.
     const int npairs = (nw + 1) / 2;
-    int starts[kMaxNb + 1];
-    int total = 0;
+    int rows_before[kMaxNb + 1];
+    int nrows = 0;
 #pragma unroll
     for (int p = 0; p < kMaxNb; p++) {
-        starts[p] = total;
+        rows_before[p] = nrows;
         if (p < npairs) {
             const int wa = 2 * p, wb = 2 * p + 1;
             const int na = npos(S.pw[wa]);
-            total += wb < nw ? max(na, npos(S.pw[wb])) : (na + 1) / 2;
+            const int slots = wb < nw ? max(na, npos(S.pw[wb])) : (na + 1) / 2;
+            nrows += (slots + 31) >> 5;
         }
     }
-    starts[kMaxNb] = total;
+    rows_before[kMaxNb] = nrows;
 
-    for (int base = 0; base < total; base += 64) {
-        // up to two slots per lane; each slot carries two candidates
+    for (int rb = 0; rb < nrows; rb += 2) {
+        // two slot rows per pass; each slot carries two candidates
         const float* tp[4];
         int rslot[4], qxy[4], win[4];
         bool valid[4];
 #pragma unroll
         for (int s2 = 0; s2 < 2; s2++) {
-            const int slot = base + lane + 32 * s2;
+            const int row = rb + s2;
             int p = 0;
 #pragma unroll
-            for (int q = 1; q < kMaxNb; q++) p += (slot >= starts[q] && q < npairs) ? 1 : 0;
-            const int j = slot - starts[p];
+            for (int q = 1; q < kMaxNb; q++) p += (row >= rows_before[q] && q < npairs) ? 1 : 0;
+            const int j = ((row - rows_before[p]) << 5) + lane;
             const int wa = 2 * p, wb = 2 * p + 1;
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -256,10 +260,15 @@ __device__ void phase_distances(const StepParams& P, const Smem& S, int nw, int 
                 win[c4] = 0;
                 rslot[c4] = 0;
                 qxy[c4] = 0;
-                if (slot >= total) continue;
+                if (row >= nrows) continue;
                 int w = wa, pos = j;
-                if (wb < nw) w = h ? wb : wa;
-                else if (h) pos = j + (npos(S.pw[wa]) + 1) / 2;
+                if (wb < nw) {
+                    w = h ? wb : wa;
+                } else {
+                    const int half = (npos(S.pw[wa]) + 1) / 2;
+                    if (j >= half) continue;
+                    if (h) pos = j + half;
+                }
                 const PWin pwn = S.pw[w];
                 if (pos < npos(pwn)) {
                     const int dy = pos_row(pos, pwn.rcp_ww), dx = pos - dy * pwn.ww;
@@ -427,13 +436,13 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
     S.scr = reinterpret_cast<Pair*>(ws + off);
     off = align16(off + sizeof(Pair) * L.scr_cap);
     S.fc = reinterpret_cast<Pair*>(ws + off);
-    off = align16(off + sizeof(Pair) * 2 * kMaxNb * kMaxNb);
+    off = align16(off + sizeof(Pair) * 2 * Nb * Nb);
     S.best = reinterpret_cast<Pair*>(ws + off);
     off = align16(off + sizeof(Pair) * P.bm_best_cap);
     S.wins = reinterpret_cast<Win*>(ws + off);
     off = align16(off + sizeof(Win) * P.bm_win_cap);
     S.pw = reinterpret_cast<PWin*>(ws + off);
-    off = align16(off + sizeof(PWin) * 2 * kMaxNb);
+    off = align16(off + sizeof(PWin) * 2 * Nb);
     S.cen = reinterpret_cast<unsigned*>(ws + off);
     off = align16(off + sizeof(unsigned) * 2 * kMaxNb);
     S.cnt = reinterpret_cast<int*>(ws + off);  // [0..2]: counters, [3..]: windows before phase window w
@@ -538,7 +547,7 @@ bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __res
         int w0 = 0;
         for (int chain = 1; chain <= 2; chain++) {
             if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
-            Pair* fc = S.fc + (chain - 1) * kMaxNb * kMaxNb;
+            Pair* fc = S.fc + (chain - 1) * Nb * Nb;
             int nfc = 0;
             for (int m = 0; m < Nb; m++) select_window(P, S, S.pw[w0 + m], lane, fc, nfc, S.scr);
             w0 += Nb;
@@ -612,10 +621,10 @@ Layout bm2_layout(const StepParams& P)
     off = align16(off + sizeof(float) * L.tile_floats);
     off = align16(off + sizeof(Pair) * L.res_cap);
     off = align16(off + sizeof(Pair) * L.scr_cap);
-    off = align16(off + sizeof(Pair) * 2 * kMaxNb * kMaxNb);
+    off = align16(off + sizeof(Pair) * 2 * P.Nb * P.Nb);
     off = align16(off + sizeof(Pair) * P.bm_best_cap);
     off = align16(off + sizeof(Win) * P.bm_win_cap);
-    off = align16(off + sizeof(PWin) * 2 * kMaxNb);
+    off = align16(off + sizeof(PWin) * 2 * P.Nb);
     off = align16(off + sizeof(unsigned) * 2 * kMaxNb);
     off = align16(off + sizeof(int) * (3 + 2 * kMaxNb));
     if (off > 24 * 1024) return L;
