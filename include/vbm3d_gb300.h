@@ -79,8 +79,8 @@ typedef struct vbm3d_dims {
 } vbm3d_dims;
 
 /* Limits of this build (a call outside them returns VBM3D_ERR_UNSUPPORTED):
- * channels in {1, 3}; 2 <= k <= 16; kt == 1 unless noted in the
- * documentation; N <= 32; Nb <= 8; Ns, Npr odd-or-even <= 15; Nf <= 32. */
+ * channels in {1, 3}; k <= 16; kt <= 4; N <= 32; Nb <= 8; Ns, Npr <= 15;
+ * Nf <= 16; W * H * F * C < 2^32 (32-bit patch indices, as the reference). */
 
 /* Default parameters of the reference CLI for step 1 (hard threshold) or
  * step 2 (Wiener) at noise level sigma, i.e. initializeParameters_1 /

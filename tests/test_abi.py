@@ -64,7 +64,7 @@ def status_of(lib, fn, *args):
 
 
 @pytest.mark.parametrize("bad,code", [
-    (dict(kt=2), 2),            # temporal patches not on the GPU yet
+    (dict(kt=5), 2),            # temporal patches above 4 frames
     (dict(T_2D=1, k=7), 1),     # bior1.5 needs k == 8
     (dict(T_2D=5), 1),
     (dict(p=0), 1),

@@ -62,7 +62,7 @@ def assert_bm_equal(got, want, p):
     np.testing.assert_array_equal(got["dist"][mask], want["dist"][mask])
 
 
-GPU_CASES = [n for n in names() if "kt2" not in n]
+GPU_CASES = names()
 
 
 @pytest.mark.parametrize("name", GPU_CASES)
@@ -96,6 +96,30 @@ def test_block_matching_synthetic(dev, oracle, shape, sigma, flow, seed):
         want = oracle.similar(p, noisy, ff, bf)
         got = gpu_similar(noisy, p, dev, ff, bf)
         assert_bm_equal(got, want, p)
+
+
+@pytest.mark.parametrize("kt,mc,t2d", [(2, 0, 0), (2, 1, 0), (3, 1, 1), (2, 1, 1)])
+def test_temporal_patches(dev, oracle, kt, mc, t2d):
+    # kt > 1 (temporal DCT when T_2D is the DCT) and motion-compensated
+    # trajectories (src/vbm3d.cpp:378-425, :1866-1956)
+    clean, noisy, ff, bf = make_clip(56, 48, 7, 3, 25.0, 50 + kt, with_flow=True)
+    p1 = oracle.default_params(1, 25.0).replace(kt=kt, mc=mc, T_2D=t2d)
+    p2 = oracle.default_params(2, 25.0).replace(kt=kt, mc=mc)
+    for p in (p1, p2):
+        assert_bm_equal(gpu_similar(noisy, p, dev, ff, bf), oracle.similar(p, noisy, ff, bf), p)
+    num, den = vb.step1(gpu(noisy, dev), p1, 25.0, gpu(ff, dev), gpu(bf, dev), True)
+    torch.cuda.synchronize()
+    onum, oden = oracle.step(1, p1, 25.0, noisy, None, ff, bf, True)
+    b_gpu = ratio(num.cpu().numpy(), den.cpu().numpy(), noisy)
+    b_ora = ratio(onum, oden, noisy)
+    assert np.abs(b_gpu - b_ora).max() <= TOL
+    num2, den2 = vb.step2(gpu(noisy, dev), gpu(b_ora, dev), p2, 25.0, gpu(ff, dev), gpu(bf, dev), True)
+    torch.cuda.synchronize()
+    o2n, o2d = oracle.step(2, p2, 25.0, noisy, b_ora, ff, bf, True)
+    assert np.abs(ratio(num2.cpu().numpy(), den2.cpu().numpy(), b_ora) - ratio(o2n, o2d, b_ora)).max() <= TOL
+    gb, gf = vb.run_host(noisy, 25.0, p1, p2, fflow=ff, bflow=bf, color_space=True)
+    ob, of = oracle.run(25.0, noisy, p1, p2, ff, bf, color_space=True, threads=4)
+    assert abs(psnr(clean, gf) - psnr(clean, of)) <= 0.01
 
 
 def test_block_matching_ties(dev, oracle):

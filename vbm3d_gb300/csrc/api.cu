@@ -22,8 +22,8 @@ cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
                       long long count, cudaStream_t stream, unsigned long long* out_count = nullptr);
 cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
-                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den, float* pair,
-                          long long count, cudaStream_t stream);
+                          const float* fflow, const unsigned* tab_idx, const unsigned* tab_nsx, float* num,
+                          float* den, float* pair, long long count, cudaStream_t stream);
 cudaError_t launch_split_pair(const float* pair, float* num, float* den, size_t n, cudaStream_t s);
 cudaError_t launch_normalize_pair(const float* pair, const float* fb, float* out, size_t n, cudaStream_t s);
 cudaError_t launch_normalize(const float* num, const float* den, const float* fb, float* out, size_t n,
@@ -208,7 +208,7 @@ int check_params(const vbm3d_params* p, vbm3d_dims d)
     if (p->T_2D == VBM3D_BIOR && p->k != 8)
         return fail(VBM3D_ERR_INVALID_ARGUMENT, "bior1.5 needs k == 8 (src/lib_transforms.cpp:137)");
     if (p->k > (unsigned)kMaxK) return fail(VBM3D_ERR_UNSUPPORTED, "k > %d", kMaxK);
-    if (p->kt != 1) return fail(VBM3D_ERR_UNSUPPORTED, "kt > 1 is not implemented on the GPU");
+    if (p->kt > (unsigned)kMaxKt) return fail(VBM3D_ERR_UNSUPPORTED, "kt > %d", kMaxKt);
     if (p->N > (unsigned)kMaxN) return fail(VBM3D_ERR_UNSUPPORTED, "N > %d", kMaxN);
     if (p->Nb > (unsigned)kMaxNb) return fail(VBM3D_ERR_UNSUPPORTED, "Nb > %d", kMaxNb);
     if (p->Ns > (unsigned)kMaxWin || p->Npr > (unsigned)kMaxWin)
@@ -308,7 +308,7 @@ int run_step_pair(int step, const StepParams& P, const float* noisy, const float
     CK(pool_alloc(&tab_nsx, (size_t)P.nrefs, s));
     CK(cudaMemsetAsync(pair, 0, 2 * n * sizeof(float), s));
     CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx, nullptr, nullptr, tab_nsx, P.nrefs, s));
-    CK(launch_filter(step, P, noisy, basic, tab_idx, tab_nsx, nullptr, nullptr, pair, P.nrefs, s));
+    CK(launch_filter(step, P, noisy, basic, fflow, tab_idx, tab_nsx, nullptr, nullptr, pair, P.nrefs, s));
     CK(cudaFreeAsync(tab_idx, s));
     CK(cudaFreeAsync(tab_nsx, s));
     return VBM3D_OK;

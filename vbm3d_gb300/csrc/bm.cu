@@ -40,12 +40,29 @@ struct WarpBM {
     int nevals;      // patchDistance evaluations so far (measurement)
 };
 
-// patchDistance for kt == 1 (src/vbm3d.cpp:965-1010).
+// patchDistance (src/vbm3d.cpp:930-1011): the reference patch is staged as
+// [ht][c][y][x] along its own trajectory; the candidate follows its own.
 __device__ __forceinline__ float cand_distance(const StepParams& P, const float* __restrict__ ref,
-                                               const float* __restrict__ vid, int qx, int qy, int t)
+                                               const float* __restrict__ vid, const float* __restrict__ fflow,
+                                               int qx, int qy, int t)
 {
     const int k = P.k;
     float s = 0.f;
+    if (P.kt > 1) {
+        int tx[kMaxKt], ty[kMaxKt];
+        trajectory(P, fflow, qx, qy, t, tx, ty);
+        for (int ht = 0; ht < P.kt; ht++)
+            for (int c = 0; c < P.C; c++) {
+                const float* pc = vid + (size_t)(t + ht) * P.whc + (size_t)c * P.wh + (size_t)ty[ht] * P.W + tx[ht];
+                const float* rc = ref + (ht * P.C + c) * k * k;
+                for (int hy = 0; hy < k; hy++)
+                    for (int hx = 0; hx < k; hx++) {
+                        const float d = rc[hy * k + hx] - __ldg(pc + (size_t)hy * P.W + hx);
+                        s = s + d * d;
+                    }
+            }
+        return s / (float)(k * k * P.kt * P.C);
+    }
     const float* base = vid + (size_t)t * P.whc + (size_t)qy * P.W + qx;
     for (int c = 0; c < P.C; c++) {
         const float* pc = base + (size_t)c * P.wh;
@@ -67,7 +84,7 @@ __device__ __forceinline__ float cand_distance(const StepParams& P, const float*
 // centred on (cx, cy) in frame t and appends its min(Nb, #unseen) best
 // candidates, sorted, to out[nout...].
 __device__ void search_window(const StepParams& P, WarpBM& w, const float* __restrict__ vid,
-                              int lane, int t, int cx, int cy, int s, int rx, int ry,
+                              const float* __restrict__ fflow, int lane, int t, int cx, int cy, int s, int rx, int ry,
                               Pair* out, int& nout)
 {
     const int half = (s - 1) / 2;
@@ -95,7 +112,7 @@ __device__ void search_window(const StepParams& P, WarpBM& w, const float* __res
                 }
             }
             if (!seen) {
-                float d = cand_distance(P, w.ref, vid, qx, qy, t);
+                float d = cand_distance(P, w.ref, vid, fflow, qx, qy, t);
                 if (qx == rx && qy == ry) d = d - P.dbias;
                 cd[j] = d;
                 cv[j] = true;
@@ -175,8 +192,8 @@ __device__ void search_window(const StepParams& P, WarpBM& w, const float* __res
 // One prediction step of the forward (dir = +1) or backward (dir = -1)
 // chain (src/vbm3d.cpp:1123-1143, :1147-1167).
 __device__ void chain_step(const StepParams& P, WarpBM& w, const float* __restrict__ vid,
-                           const float* __restrict__ flow, unsigned* centres, int dir, int lane,
-                           int rx, int ry, int& nbest)
+                           const float* __restrict__ flow, const float* __restrict__ fflow, unsigned* centres, int dir,
+                           int lane, int rx, int ry, int& nbest)
 {
     const int k = P.k;
     int nfc = 0;
@@ -191,7 +208,7 @@ __device__ void chain_step(const StepParams& P, WarpBM& w, const float* __restri
         const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + k / 2) * P.W + px + k / 2) : 0.f;
         int ny = (int)((float)py + roundf(fy));
         py = min(max(ny, 0), P.H - k);
-        search_window(P, w, vid, lane, pt + dir, px, py, P.Npr, rx, ry, w.fc, nfc);
+        search_window(P, w, vid, fflow, lane, pt + dir, px, py, P.Npr, rx, ry, w.fc, nfc);
     }
     const int m2 = min(P.Nb, nfc);
     if (lane == 0) {
@@ -220,7 +237,7 @@ bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __rest
     const int k = P.k, k2 = k * k;
     WarpBM w;
     w.ref = reinterpret_cast<float*>(ws);
-    size_t off = ((size_t)P.C * k2 * sizeof(float) + 15) & ~size_t(15);
+    size_t off = ((size_t)P.C * P.kt * k2 * sizeof(float) + 15) & ~size_t(15);
     w.list = reinterpret_cast<Pair*>(ws + off);
     off += (size_t)P.bm_list_cap * sizeof(Pair);
     w.best = reinterpret_cast<Pair*>(ws + off);
@@ -236,14 +253,20 @@ bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __rest
 
     int rx, ry, rt;
     ref_coords(P, r, rx, ry, rt);
-    for (int e = lane; e < P.C * k2; e += 32) {
-        const int c = e / k2, pq = e - c * k2, py = pq / k, px = pq - py * k;
-        w.ref[e] = __ldg(vid + (size_t)rt * P.whc + (size_t)c * P.wh + (size_t)(ry + py) * P.W + rx + px);
+    {
+        int tx[kMaxKt], ty[kMaxKt];
+        trajectory(P, fflow, rx, ry, rt, tx, ty);
+        for (int e = lane; e < P.kt * P.C * k2; e += 32) {
+            const int sl = e / k2, pq = e - sl * k2, ht = sl / P.C, c = sl - ht * P.C;
+            const int py = pq / k, px = pq - py * k;
+            w.ref[e] = __ldg(vid + (size_t)(rt + ht) * P.whc + (size_t)c * P.wh + (size_t)(ty[ht] + py) * P.W +
+                             tx[ht] + px);
+        }
     }
     __syncwarp();
 
     int nbest = 0;
-    search_window(P, w, vid, lane, rt, rx, ry, P.Ns, rx, ry, w.best, nbest);
+    search_window(P, w, vid, fflow, lane, rt, rx, ry, P.Ns, rx, ry, w.best, nbest);
     if (lane < P.Nb) {
         // the reference reads bestPatches[i] for every i < Nb
         // (src/vbm3d.cpp:1115-1119); the host rejects grids where the
@@ -254,9 +277,9 @@ bm_kernel(const StepParams P, const float* __restrict__ vid, const float* __rest
     __syncwarp();
 
     const int fend = min(rt + P.Nf, P.F - P.kt) - rt;
-    for (int f = 0; f < fend; f++) chain_step(P, w, vid, fflow, w.post, +1, lane, rx, ry, nbest);
+    for (int f = 0; f < fend; f++) chain_step(P, w, vid, fflow, fflow, w.post, +1, lane, rx, ry, nbest);
     const int bend = min(rt, P.Nf);
-    for (int f = 0; f < bend; f++) chain_step(P, w, vid, bflow, w.pre, -1, lane, rx, ry, nbest);
+    for (int f = 0; f < bend; f++) chain_step(P, w, vid, bflow, fflow, w.pre, -1, lane, rx, ry, nbest);
 
     if (lane == 0) {
         const int nsimp = min(P.N, nbest);
@@ -284,7 +307,7 @@ int bm_warp_bytes(const StepParams& P, int& list_cap, int& best_cap, int& win_ca
     list_cap = win * win;
     best_cap = P.Nb * (1 + 2 * P.Nf);
     win_cap = 1 + 2 * P.Nf * P.Nb;
-    size_t off = ((size_t)P.C * P.k * P.k * sizeof(float) + 15) & ~size_t(15);
+    size_t off = ((size_t)P.C * P.kt * P.k * P.k * sizeof(float) + 15) & ~size_t(15);
     off += (size_t)list_cap * sizeof(Pair) + (size_t)best_cap * sizeof(Pair);
     off += (size_t)kMaxNb * kMaxNb * sizeof(Pair) + 2 * kMaxNb * sizeof(unsigned);
     off += (size_t)win_cap * sizeof(Win);

@@ -25,6 +25,7 @@ constexpr int kMaxNb = 8;        // matches kept per frame
 constexpr int kMaxWin = 15;      // search window side (Ns, Npr)
 constexpr int kMaxNf = 16;       // frames searched each way
 constexpr int kMaxC = 3;         // channels
+constexpr int kMaxKt = 4;        // temporal patch size
 constexpr int kSlots = 8;        // window candidates per lane: 32*8 >= 15*15
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -90,10 +91,45 @@ __device__ __forceinline__ void patch_coords(const StepParams& P, unsigned idx, 
     x = (int)(r - (unsigned)y * (unsigned)P.W);
 }
 
+// patch_trajectory (src/vbm3d.cpp:378-425, FLOAT_TRAJECTORIES): the
+// top-left corner of the patch's slice ht, for ht < kt.  Static unless mc;
+// with mc the corner follows the forward flow read at the previous corner,
+// accumulated in float and rounded (half away from zero) and clamped.
+__device__ __forceinline__ void trajectory(const StepParams& P, const float* __restrict__ fflow, int px, int py,
+                                           int pt, int* tx, int* ty)
+{
+    float fpx = (float)px, fpy = (float)py;
+    for (int ht = 0; ht < P.kt; ht++) {
+        tx[ht] = px;
+        ty[ht] = py;
+        if (P.mc && ht < P.kt - 1) {
+            float fx = 0.f, fy = 0.f;
+            if (fflow) {
+                const float* fl = fflow + (size_t)(pt + ht) * 2 * P.wh + (size_t)(py + P.k / 2) * P.W + px + P.k / 2;
+                fx = __ldg(fl);
+                fy = __ldg(fl + P.wh);
+            }
+            fpx = fpx + fx;
+            fpy = fpy + fy;
+            px = min(P.W - P.k, max(0, (int)roundf(fpx)));
+            py = min(P.H - P.k, max(0, (int)roundf(fpy)));
+        }
+    }
+}
+
 // (float)((double)s * SQRT2_INV) with float arithmetic (see kS2iHi).
 __device__ __forceinline__ float mul_sqrt2_inv(float s)
 {
     return __fmaf_rn(s, kS2iHi, __fmul_rn(s, kS2iLo));
+}
+
+// (float)((double)s * SQRT2) likewise, SQRT2 being the reference's double
+// literal 1.414213562373095 (src/vbm3d.cpp:32).
+constexpr float kS2Hi = 1.41421353816986084f;       // float(1.414213562373095)
+constexpr float kS2Lo = 2.4203234972131361e-08f;    // float(1.414213562373095 - kS2Hi)
+__device__ __forceinline__ float mul_sqrt2(float s)
+{
+    return __fmaf_rn(s, kS2Hi, __fmul_rn(s, kS2Lo));
 }
 
 struct Pair {

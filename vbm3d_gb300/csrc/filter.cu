@@ -297,35 +297,38 @@ template <int STEP, int NMAX = 32>
 __device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* gB, int nsx, int ss, int lane,
                                         float* wgt)
 {
-    const int k2 = P.k * P.k, C = P.C;
-    // 1D transform along the group + shrinkage, one (c, pq) per lane
+    // slices are laid out [c][n][ht][k*k] with stride ss; the coefficient
+    // vector (c, ht, pq) runs over n with stride kt*ss.  Its index in the
+    // reference's group_3D is pq + ht*k*k, so the group DC is pq = ht = 0.
+    const int k2 = P.k * P.k, kt = P.kt, k2t = k2 * kt, C = P.C, ns = kt * ss;
     float acc[kMaxC] = {0.f, 0.f, 0.f};
-    for (int v = lane; v < C * k2; v += 32) {
-        const int c = v / k2, pq = v - c * k2;
-        float* ga = gA + (size_t)(c * nsx) * ss + pq;
-        float* gb = gB + (size_t)(c * nsx) * ss + pq;
+    for (int v = lane; v < C * k2t; v += 32) {
+        const int c = v / k2t, rem = v - c * k2t, ht = rem / k2, pq = rem - ht * k2;
+        float* ga = gA + ((size_t)(c * nsx) * kt + ht) * ss + pq;
+        float* gb = gB + ((size_t)(c * nsx) * kt + ht) * ss + pq;
+        const bool dc = pq == 0 && ht == 0;
         if (STEP == 1) {
             const float T = P.lambda3D * P.sigma[c] * (P.T3D == kHADAMARD ? sqrtf((float)nsx) : 1.0f);
             int kept;
             switch (nsx) {
-                case 1: kept = ht_vector<1>(ga, ss, pq == 0, T, P.T3D); break;
-                case 2: kept = ht_vector<2>(ga, ss, pq == 0, T, P.T3D); break;
-                case 4: kept = ht_vector<4>(ga, ss, pq == 0, T, P.T3D); break;
-                case 8: kept = ht_vector<(NMAX < 8 ? NMAX : 8)>(ga, ss, pq == 0, T, P.T3D); break;
-                case 16: kept = ht_vector<(NMAX < 16 ? NMAX : 16)>(ga, ss, pq == 0, T, P.T3D); break;
-                default: kept = ht_vector<NMAX>(ga, ss, pq == 0, T, P.T3D); break;
+                case 1: kept = ht_vector<1>(ga, ns, dc, T, P.T3D); break;
+                case 2: kept = ht_vector<2>(ga, ns, dc, T, P.T3D); break;
+                case 4: kept = ht_vector<4>(ga, ns, dc, T, P.T3D); break;
+                case 8: kept = ht_vector<(NMAX < 8 ? NMAX : 8)>(ga, ns, dc, T, P.T3D); break;
+                case 16: kept = ht_vector<(NMAX < 16 ? NMAX : 16)>(ga, ns, dc, T, P.T3D); break;
+                default: kept = ht_vector<NMAX>(ga, ns, dc, T, P.T3D); break;
             }
             acc[c] += (float)kept;
         } else {
             const float s2 = P.sigma[c] * P.sigma[c];
             float ws;
             switch (nsx) {
-                case 1: ws = wiener_vector<1>(ga, gb, ss, s2, P.T3D); break;
-                case 2: ws = wiener_vector<2>(ga, gb, ss, s2, P.T3D); break;
-                case 4: ws = wiener_vector<4>(ga, gb, ss, s2, P.T3D); break;
-                case 8: ws = wiener_vector<(NMAX < 8 ? NMAX : 8)>(ga, gb, ss, s2, P.T3D); break;
-                case 16: ws = wiener_vector<(NMAX < 16 ? NMAX : 16)>(ga, gb, ss, s2, P.T3D); break;
-                default: ws = wiener_vector<NMAX>(ga, gb, ss, s2, P.T3D); break;
+                case 1: ws = wiener_vector<1>(ga, gb, ns, s2, P.T3D); break;
+                case 2: ws = wiener_vector<2>(ga, gb, ns, s2, P.T3D); break;
+                case 4: ws = wiener_vector<4>(ga, gb, ns, s2, P.T3D); break;
+                case 8: ws = wiener_vector<(NMAX < 8 ? NMAX : 8)>(ga, gb, ns, s2, P.T3D); break;
+                case 16: ws = wiener_vector<(NMAX < 16 ? NMAX : 16)>(ga, gb, ns, s2, P.T3D); break;
+                default: ws = wiener_vector<NMAX>(ga, gb, ns, s2, P.T3D); break;
             }
             acc[c] += ws;
         }
@@ -341,56 +344,110 @@ __device__ __forceinline__ void group_1d(const StepParams& P, float* gA, float* 
 
 }
 
-// Any k <= 16: slices transformed in shared memory with runtime-sized loops.
+// temporal_transform / temporal_inv_transform (src/vbm3d.cpp:1866-1956):
+// an orthonormal DCT-II along the kt slices of every (c, n, pq), for
+// kt > 1 with the DCT 2D transform.  Forward: REDFT10 * norm, and the
+// first coefficient times SQRT2_INV through double as in the reference;
+// inverse: the first coefficient times SQRT2 through double, REDFT01, * norm.
+__device__ void temporal_group(const StepParams& P, float* g, int nsx, int ss, int lane, bool inverse)
+{
+    const int kt = P.kt, k2 = P.k * P.k, total = P.C * nsx * k2;
+    const float norm = (float)(1. / sqrt(2.0 * kt));
+    const float pi = 3.14159265358979f;
+    for (int v = lane; v < total; v += 32) {
+        const int cn = v / k2, pq = v - cn * k2;  // cn = c * nsx + n
+        float* base = g + (size_t)cn * kt * ss + pq;
+        float in[kMaxKt], out[kMaxKt];
+        for (int t = 0; t < kt; t++) in[t] = base[t * ss];
+        if (!inverse) {
+            for (int u = 0; u < kt; u++) {
+                float m = 0.f;
+                for (int t = 0; t < kt; t++) m = __fmaf_rn(in[t], 2.0f * cosf(pi * (t + 0.5f) * u / kt), m);
+                const float y = m * norm;
+                out[u] = u == 0 ? mul_sqrt2_inv(y) : y;
+            }
+        } else {
+            in[0] = mul_sqrt2(in[0]);
+            for (int t = 0; t < kt; t++) {
+                float m = in[0];
+                for (int u = 1; u < kt; u++) m = __fmaf_rn(in[u], 2.0f * cosf(pi * u * (t + 0.5f) / kt), m);
+                out[t] = m * norm;
+            }
+        }
+        for (int t = 0; t < kt; t++) base[t * ss] = out[t];
+    }
+}
+
+// Any k <= 16 and kt <= 4: slices [c][n][ht] transformed in shared memory
+// with runtime-sized loops; slice ht of patch n follows the patch's
+// trajectory (patch_trajectory, src/vbm3d.cpp:378-425).
 template <int STEP, bool PAIR>
 __global__ void __launch_bounds__(128)
 filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
-                      const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
-                      const AggTarget A, int warp_floats)
+                      const float* __restrict__ fflow, const unsigned* __restrict__ tab_idx,
+                      const unsigned* __restrict__ tab_nsx, const AggTarget A, int warp_floats)
 {
     extern __shared__ __align__(16) float fsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
     if (r >= P.nrefs) return;
 
-    const int k = P.k, k2 = k * k, C = P.C;
+    const int k = P.k, k2 = k * k, C = P.C, kt = P.kt;
     const int ss = k2 + 1;  // slice stride
     float* base = fsm + (size_t)wid * warp_floats;
-    unsigned* idx = reinterpret_cast<unsigned*>(base);
-    float* gA = base + kMaxN;                 // noisy group (step 1: the group)
-    float* gT = gA + (size_t)C * P.N * ss;    // per-slice scratch
-    float* gB = gT + (size_t)C * P.N * ss;    // basic group (step 2)
+    int* traj = reinterpret_cast<int*>(base);                // [n][ht]: top-left offset in channel 0
+    float* gA = base + kMaxN * kMaxKt;                      // noisy group (step 1: the group)
+    float* gT = gA + (size_t)C * P.N * kt * ss;             // per-slice scratch
+    float* gB = gT + (size_t)C * P.N * kt * ss;             // basic group (step 2)
 
     const int nsx = (int)tab_nsx[r];
-    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
+    if (lane < nsx) {
+        int x, y, t, tx[kMaxKt], ty[kMaxKt];
+        patch_coords(P, tab_idx[(size_t)r * P.N + lane], x, y, t);
+        trajectory(P, fflow, x, y, t, tx, ty);
+        for (int ht = 0; ht < kt; ht++) traj[lane * kMaxKt + ht] = (int)patch_index(P, tx[ht], ty[ht], t + ht);
+    }
     __syncwarp();
 
-    gather(P, noisy, idx, nsx, ss, gA, lane);
-    if (STEP == 2) gather(P, basic, idx, nsx, ss, gB, lane);
+    const int nsl = C * nsx * kt;  // slice sl = (c * nsx + n) * kt + ht
+    for (int e = lane; e < nsl * k2; e += 32) {
+        const int sl = e / k2, pq = e - sl * k2;
+        const int cn = sl / kt, ht = sl - cn * kt, c = cn / nsx, n = cn - c * nsx;
+        const int p = pq / k, q = pq - p * k;
+        const size_t o = (size_t)traj[n * kMaxKt + ht] + (size_t)c * P.wh + (size_t)p * P.W + q;
+        gA[sl * ss + pq] = __ldg(noisy + o);
+        if (STEP == 2) gB[sl * ss + pq] = __ldg(basic + o);
+    }
     __syncwarp();
-    const int nsl = C * nsx;
     for (int sl = lane; sl < nsl; sl += 32) {
         fwd2d(gA + sl * ss, gT + sl * ss, P);
         if (STEP == 2) fwd2d(gB + sl * ss, gT + sl * ss, P);
     }
     __syncwarp();
+    const bool temporal = kt > 1 && P.T2D != kBIOR;
+    if (temporal) {
+        temporal_group(P, gA, nsx, ss, lane, false);
+        if (STEP == 2) temporal_group(P, gB, nsx, ss, lane, false);
+        __syncwarp();
+    }
 
     float wgt[kMaxC];
     group_1d<STEP>(P, gA, gB, nsx, ss, lane, wgt);
 
     float* ge = STEP == 1 ? gA : gB;
+    if (temporal) {
+        temporal_group(P, ge, nsx, ss, lane, true);
+        __syncwarp();
+    }
     for (int sl = lane; sl < nsl; sl += 32) inv2d(ge + sl * ss, gT + sl * ss, P);
     __syncwarp();
 
     // aggregation (src/vbm3d.cpp:612-650): num += kaiser * w * est; den += kaiser * w
-    const int total = nsl * k2;
-    for (int e = lane; e < total; e += 32) {
+    for (int e = lane; e < nsl * k2; e += 32) {
         const int sl = e / k2, pq = e - sl * k2;
-        const int c = sl / nsx, n = sl - c * nsx;
+        const int cn = sl / kt, ht = sl - cn * kt, c = cn / nsx, n = cn - c * nsx;
         const int p = pq / k, q = pq - p * k;
-        int x, y, t;
-        patch_coords(P, idx[n], x, y, t);
-        const size_t o = (size_t)t * P.whc + (size_t)c * P.wh + (size_t)(y + p) * P.W + x + q;
+        const size_t o = (size_t)traj[n * kMaxKt + ht] + (size_t)c * P.wh + (size_t)p * P.W + q;
         const float kw = P.kaiser[pq] * wgt[c];
         agg_add<PAIR>(A, o, kw * ge[sl * ss + pq], kw);
     }
@@ -589,33 +646,37 @@ cudaError_t launch_k(const StepParams& P, const float* noisy, const float* basic
 }
 
 template <int STEP, bool PAIR>
-cudaError_t launch_generic(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
-                           const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+cudaError_t launch_generic(const StepParams& P, const float* noisy, const float* basic, const float* fflow,
+                           const unsigned* tab_idx, const unsigned* tab_nsx, const AggTarget& A, long long count,
+                           cudaStream_t stream)
 {
-    const int warps = 4;
-    const int wf = kMaxN + (STEP == 1 ? 2 : 3) * P.C * P.N * (P.k * P.k + 1);  // group(s) + scratch
+    // group(s) + scratch, kt slices per patch, plus the trajectories
+    const int wf = kMaxN * kMaxKt + (STEP == 1 ? 2 : 3) * P.C * P.N * P.kt * (P.k * P.k + 1);
+    int warps = 4;
+    while (warps > 1 && (size_t)warps * wf * sizeof(float) > 200 * 1024) warps /= 2;
     const size_t smem = (size_t)warps * wf * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(filter_kernel_generic<STEP, PAIR>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (count + warps - 1) / warps;
-    filter_kernel_generic<STEP, PAIR><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
-                                                                                     tab_nsx, A, wf);
+    filter_kernel_generic<STEP, PAIR><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, fflow,
+                                                                                     tab_idx, tab_nsx, A, wf);
     return cudaGetLastError();
 }
 
 template <int STEP, bool PAIR>
-cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
-                     const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic, const float* fflow,
+                     const unsigned* tab_idx, const unsigned* tab_nsx, const AggTarget& A, long long count,
+                     cudaStream_t stream)
 {
-    if (P.N <= 8) {  // group sizes up to 8: the register-resident kernel
+    if (P.N <= 8 && P.kt == 1) {  // group sizes up to 8, 2D patches: the register-resident kernel
         switch (P.k) {
             case 7: return launch_k<STEP, 7, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
             case 8: return launch_k<STEP, 8, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
             default: break;
         }
     }
-    return launch_generic<STEP, PAIR>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    return launch_generic<STEP, PAIR>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream);
 }
 
 }  // namespace
@@ -623,15 +684,15 @@ cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic
 // Aggregates into num / den when `pair` is NULL, else into the interleaved
 // (num, den) array `pair` (2 floats per video value).
 cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
-                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den, float* pair,
-                          long long count, cudaStream_t stream)
+                          const float* fflow, const unsigned* tab_idx, const unsigned* tab_nsx, float* num,
+                          float* den, float* pair, long long count, cudaStream_t stream)
 {
     const AggTarget A{num, den, pair};
     if (step == 1)
-        return pair ? dispatch<1, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
-                    : dispatch<1, false>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
-    return pair ? dispatch<2, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
-                : dispatch<2, false>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+        return pair ? dispatch<1, true>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream)
+                    : dispatch<1, false>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream);
+    return pair ? dispatch<2, true>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream)
+                : dispatch<2, false>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream);
 }
 
 }  // namespace vbm3d

@@ -28,8 +28,8 @@ cudaError_t launch_bm(const StepParams& P, const float* vid, const float* fflow,
                       unsigned* out_idx, float* out_dist, unsigned* out_nsimp, unsigned* out_nsx,
                       long long count, cudaStream_t stream, unsigned long long* out_count);
 cudaError_t launch_filter(int step, const StepParams& P, const float* noisy, const float* basic,
-                          const unsigned* tab_idx, const unsigned* tab_nsx, float* num, float* den, float* pair,
-                          long long count, cudaStream_t stream);
+                          const float* fflow, const unsigned* tab_idx, const unsigned* tab_nsx, float* num,
+                          float* den, float* pair, long long count, cudaStream_t stream);
 int build_step_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_space, StepParams& P);
 void set_last_error(int status, const char* msg);
 }  // namespace vbm3d
@@ -110,7 +110,8 @@ extern "C" int vbm3d_gpu_step1_noalloc(const vbm3d_params* prms, const float* no
     if (e == cudaSuccess) e = vbm3d::launch_bm(P, noisy, fflow, bflow, tab_idx, nullptr, nullptr, tab_nsx, P.nrefs, s,
                                                nullptr);
     if (e == cudaSuccess)
-        e = vbm3d::launch_filter(1, P, noisy, nullptr, tab_idx, tab_nsx, numerator, denominator, nullptr, P.nrefs, s);
+        e = vbm3d::launch_filter(1, P, noisy, nullptr, fflow, tab_idx, tab_nsx, numerator, denominator, nullptr,
+                                 P.nrefs, s);
     if (e != cudaSuccess) {
         vbm3d::set_last_error(VBM3D_ERR_CUDA, cudaGetErrorString(e));
         return VBM3D_ERR_CUDA;
