@@ -188,6 +188,26 @@ int vbm3d_gpu_similar_patches(const vbm3d_params *prms, const float *video,
                               unsigned *nsimp, unsigned *nsx,
                               size_t *n_refs, void *stream);
 
+/* Frozen linearisation of one step and its adjoint (no reference
+ * counterpart; the differentiation form of the filter).  With the
+ * block-matching groups, the hard-threshold masks (step 1) or Wiener gains
+ * (step 2) and the aggregation weights frozen at their forward-pass values,
+ * a step's output is a linear map L of its noisy input; applied to the
+ * noisy input itself it is the forward step.
+ *   vbm3d_linear_create: runs the step's block matching and forward filter
+ *     on (noisy, basic) and keeps the groups and the denominator; `noisy`
+ *     (and `basic` for step 2) must stay valid until vbm3d_linear_destroy.
+ *   vbm3d_linear_apply: out = L x (adjoint == 0) or out = L^T x.
+ * Limits: k in {7, 8}, kt == 1, N <= 8.  Device pointers, stream-ordered;
+ * create allocates the state with cudaMalloc. */
+typedef struct vbm3d_linear vbm3d_linear;
+int vbm3d_linear_create(int step, const vbm3d_params *prms, const float *noisy, const float *basic,
+                        const float *fflow, const float *bflow, vbm3d_dims dims, float sigma,
+                        int color_space, vbm3d_linear **state, void *stream);
+int vbm3d_linear_apply(vbm3d_linear *state, const float *x, float *out, int adjoint, void *stream);
+int vbm3d_linear_den(vbm3d_linear *state, const float **denominator);
+void vbm3d_linear_destroy(vbm3d_linear *state);
+
 /* Measurement helper with no reference counterpart: runs the block
  * matching of vbm3d_gpu_similar_patches and returns in *count the total
  * number of patch distances it evaluated (calls of the reference's

@@ -60,6 +60,8 @@ class Oracle:
         L.oracle_run.argtypes = [C.c_float, _fp, _fp, _fp, _fp, _fp, C.POINTER(Params),
                                  C.POINTER(Params), C.c_int, Dims, C.c_int]
         L.oracle_color_transform.argtypes = [_fp, Dims, C.c_int]
+        L.oracle_linear_apply.argtypes = [C.c_int, C.POINTER(Params), _fp, _fp, _fp, _fp, Dims, C.c_float, C.c_int,
+                                          _fp, C.POINTER(C.c_double), C.c_int]
         for name in ("oracle_dct2d_forward", "oracle_dct2d_inverse"):
             getattr(L, name).argtypes = [_fp, _fp, C.c_uint]
         for name in ("oracle_bior2d_forward", "oracle_bior2d_inverse"):
@@ -131,6 +133,17 @@ class Oracle:
                                  C.byref(p1), C.byref(p2), int(color_space), dims_of(nz), threads)
         assert rc == 0, rc
         return basic, den
+
+    def linear(self, step, p, sigma, noisy, x, basic=None, fflow=None, bflow=None, color_space=False, threads=4):
+        """FP64 frozen linearised step applied to x."""
+        noisy = np.ascontiguousarray(noisy, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros(noisy.shape, np.float64)
+        rc = self.lib.oracle_linear_apply(step, C.byref(p), _f(noisy), _f(basic), _f(fflow), _f(bflow), dims_of(noisy),
+                                          sigma, int(color_space), _f(x), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                          threads)
+        assert rc == 0, rc
+        return out
 
     def color_transform(self, video, forward):
         v = np.array(video, np.float32, copy=True, order="C")

@@ -984,3 +984,236 @@ out:
     free(den);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* Frozen linearisation of one step, in double precision              */
+/* ------------------------------------------------------------------ */
+
+/* 1D transforms in double: haar_forward / haar_inverse and the reference's
+ * Walsh-Hadamard (src/lib_transforms.cpp:410-512). */
+static void od_haar(double *v, unsigned n, int inverse)
+{
+    double tmp[64];
+    const double s = 0.7071067811865475;
+    if (!inverse) {
+        for (int k = (int)n / 2; k >= 1; k /= 2) {
+            for (int i = 0; i < k; i++) {
+                tmp[i] = (v[2 * i] + v[2 * i + 1]) * s;
+                tmp[i + k] = (v[2 * i] - v[2 * i + 1]) * s;
+            }
+            for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
+        }
+    } else {
+        for (int k = 1; k * 2 <= (int)n; k *= 2) {
+            for (int i = 0; i < k; i++) {
+                tmp[2 * i] = (v[i] + v[i + k]) * s;
+                tmp[2 * i + 1] = (v[i] - v[i + k]) * s;
+            }
+            for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
+        }
+    }
+}
+
+static void od_hadamard(double *v, unsigned n)
+{
+    if (n == 1) return;
+    double tmp[64];
+    const unsigned h = n / 2;
+    for (unsigned k = 0; k < h; k++) {
+        tmp[k] = v[2 * k] + v[2 * k + 1];
+        tmp[h + k] = v[2 * k] - v[2 * k + 1];
+    }
+    od_hadamard(tmp, h);
+    od_hadamard(tmp + h, h);
+    for (unsigned k = 0; k < n; k++) v[k] = tmp[k];
+}
+
+/* 2D transforms of one k x k block in double with the float-valued
+ * coefficients of the forward pass (bior1.5 bases, DCT normalisations). */
+static void od_2d(const double *in, double *out, unsigned k, unsigned t2d, int inverse)
+{
+    float cn[256], cni[256];
+    oc_coef_norm(k, cn, cni);
+    if (t2d == OC_BIOR) {
+        double b[8][8], t[64], t2[64];
+        for (int j = 0; j < 8; j++)
+            for (int q = 0; q < 8; q++) b[j][q] = (double)(float)(inverse ? OC_BIOR_INV[j][q] : OC_BIOR_FWD[j][q]);
+        for (int i = 0; i < 8; i++)
+            for (int j = 0; j < 8; j++) t[i * 8 + j] = inverse ? in[i + j * 8] : in[i * 8 + j];
+        for (int i = 0; i < 8; i++)
+            for (int j = 0; j < 8; j++) {
+                double m = 0;
+                for (int q = 0; q < 8; q++) m += t[i * 8 + q] * b[j][q];
+                t2[i * 8 + j] = m;
+            }
+        for (int i = 0; i < 8; i++)
+            for (int j = 0; j < 8; j++) {
+                double m = 0;
+                for (int q = 0; q < 8; q++) m += t2[q * 8 + i] * b[j][q];
+                if (inverse) out[j * 8 + i] = m;
+                else out[i * 8 + j] = m;
+            }
+        return;
+    }
+    const double pi = 3.14159265358979323846;
+    double m[16][16], t[256];
+    for (unsigned u = 0; u < k; u++)
+        for (unsigned j = 0; j < k; j++)
+            m[u][j] = inverse ? (u == 0 ? 1.0 : 2.0 * cos(pi * u * (j + 0.5) / k)) : 2.0 * cos(pi * (j + 0.5) * u / k);
+    double z[256];
+    for (unsigned e = 0; e < k * k; e++) z[e] = inverse ? in[e] * (double)cni[e] : in[e];
+    /* rows then columns: Y = M Z M^T, with M[u][j] the 1D transform matrix
+     * (REDFT10: Y[u] = sum_j X[j] m[u][j]; REDFT01: X[j] = sum_u Z[u] m[u][j]) */
+    for (unsigned i = 0; i < k; i++)
+        for (unsigned v = 0; v < k; v++) {
+            double a = 0;
+            for (unsigned j = 0; j < k; j++) a += z[i * k + j] * (inverse ? m[j][v] : m[v][j]);
+            t[i * k + v] = a;
+        }
+    for (unsigned u = 0; u < k; u++)
+        for (unsigned v = 0; v < k; v++) {
+            double a = 0;
+            for (unsigned i = 0; i < k; i++) a += (inverse ? m[i][u] : m[u][i]) * t[i * k + v];
+            out[u * k + v] = inverse ? a * (double)(1.0f / (float)(k * 2)) : a * (double)cn[u * k + v];
+        }
+}
+
+int oracle_linear_apply(int step, const vbm3d_params *p, const float *noisy, const float *basic,
+                        const float *fflow, const float *bflow, vbm3d_dims d, float sigma, int color_space,
+                        const float *x, double *out, int threads)
+{
+    if ((step != 1 && step != 2) || oc_check(p, d) || p->kt != 1) return 1;
+    float sig[3];
+    if (oracle_sigma_table(sigma, d.channels, color_space, sig)) return 5;
+    const float *src = step == 1 ? noisy : basic;
+    oc_ctx c;
+    oc_ctx_init(&c, p, src, fflow, bflow, d);
+    const unsigned k = p->k, k2 = k * k, C = d.channels;
+    unsigned *rows = (unsigned *)malloc(sizeof(unsigned) * (d.height + 2));
+    unsigned *cols = (unsigned *)malloc(sizeof(unsigned) * (d.width + 2));
+    unsigned nr, nc;
+    oracle_grid(p, d, &nr, &nc, rows, cols);
+    float kai[256], cn[256], cni[256];
+    oracle_kaiser(k, kai);
+    oc_coef_norm(k, cn, cni);
+    const size_t total = (size_t)c.whc * d.frames;
+    double *num = (double *)calloc(total, sizeof(double)), *den = (double *)calloc(total, sizeof(double));
+    const size_t per_ref = (size_t)C * p->N * k2;
+    double *est = (double *)malloc(sizeof(double) * per_ref * nc);
+    oc_ref_out *ro = (oc_ref_out *)malloc(sizeof(oc_ref_out) * nc);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    for (unsigned tr = 0; tr < d.frames; ++tr)
+        for (unsigned ir = 0; ir < nr; ir++) {
+#pragma omp parallel for schedule(dynamic, 4)
+            for (long jr = 0; jr < (long)nc; jr++) {
+                unsigned pidx = (unsigned)oc_index(&c, cols[jr], rows[ir], tr, 0);
+                float dd[32];
+                unsigned ns;
+                const unsigned nsx = oc_similar(&c, pidx, dd, ro[jr].idx, &ns);
+                ro[jr].nsx = nsx;
+                /* frozen gains from the source group, float as the forward */
+                float *g = (float *)malloc(sizeof(float) * C * k2 * nsx);
+                oc_build_group(&c, src, ro[jr].idx, nsx, cn, g);
+                double *lam = (double *)malloc(sizeof(double) * C * k2 * nsx);
+                float wt[3] = {0.f, 0.f, 0.f};
+                const float coefn = 1.0f / (float)nsx;
+                for (unsigned ch = 0; ch < C; ch++)
+                    for (unsigned q = 0; q < k2; q++) {
+                        float *v = g + (ch * k2 + q) * nsx;
+                        if (p->T_3D == OC_HADAMARD) oc_hadamard(v, nsx);
+                        else oracle_haar_forward(v, nsx);
+                        for (unsigned n = 0; n < nsx; n++) {
+                            double l;
+                            if (step == 1) {
+                                const float T = p->lambda3D * sig[ch] * (p->T_3D == OC_HADAMARD ? sqrtf((float)nsx) : 1.0f);
+                                l = ((q == 0 && n == 0) || fabsf(v[n]) > T) ? 1.0 : 0.0;
+                                wt[ch] += (float)l;
+                            } else if (p->T_3D == OC_HADAMARD) {
+                                float value = v[n] * v[n] * coefn;
+                                value /= (value + sig[ch] * sig[ch]);
+                                l = (double)value * (double)coefn;
+                                wt[ch] += value * value;
+                            } else {
+                                float value = v[n] * v[n];
+                                value /= (value + sig[ch] * sig[ch]);
+                                l = value;
+                                wt[ch] += value * value;
+                            }
+                            lam[(ch * k2 + q) * nsx + n] = l;
+                        }
+                    }
+                for (unsigned ch = 0; ch < C; ch++) {
+                    if (step == 2 && p->T_3D == OC_HADAMARD)
+                        ro[jr].w[ch] = wt[ch] > 0.0f ? 1.0f / (float)(sig[ch] * sig[ch] * wt[ch]) : 1.0f;
+                    else
+                        ro[jr].w[ch] = 1.f / (float)(sig[ch] * sig[ch] * wt[ch]);
+                }
+                /* the linear map on x, in double */
+                double *gx = (double *)malloc(sizeof(double) * C * k2 * nsx);
+                double blk[256], tr2[256];
+                for (unsigned ch = 0; ch < C; ch++)
+                    for (unsigned n = 0; n < nsx; n++) {
+                        unsigned px, py, pt;
+                        oc_coords(&c, ro[jr].idx[n], &px, &py, &pt);
+                        for (unsigned pp = 0; pp < k; pp++)
+                            for (unsigned q = 0; q < k; q++) blk[pp * k + q] = x[oc_index(&c, px + q, py + pp, pt, ch)];
+                        od_2d(blk, tr2, k, p->T_2D, 0);
+                        for (unsigned q = 0; q < k2; q++) gx[(ch * k2 + q) * nsx + n] = tr2[q];
+                    }
+                for (unsigned v = 0; v < C * k2; v++) {
+                    double *xv = gx + v * nsx;
+                    const double *lv = lam + v * nsx;
+                    if (p->T_3D == OC_HADAMARD) {
+                        od_hadamard(xv, nsx);
+                        for (unsigned n = 0; n < nsx; n++) xv[n] *= lv[n];
+                        od_hadamard(xv, nsx);
+                        if (step == 1)
+                            for (unsigned n = 0; n < nsx; n++) xv[n] *= (double)coefn;
+                    } else {
+                        od_haar(xv, nsx, 0);
+                        for (unsigned n = 0; n < nsx; n++) xv[n] *= lv[n];
+                        od_haar(xv, nsx, 1);
+                    }
+                }
+                double *e = est + (size_t)jr * per_ref;
+                for (unsigned ch = 0; ch < C; ch++)
+                    for (unsigned n = 0; n < nsx; n++) {
+                        for (unsigned q = 0; q < k2; q++) blk[q] = gx[(ch * k2 + q) * nsx + n];
+                        od_2d(blk, tr2, k, p->T_2D, 1);
+                        for (unsigned q = 0; q < k2; q++) e[(size_t)ch * nsx * k2 + (size_t)n * k2 + q] = tr2[q];
+                    }
+                free(g);
+                free(lam);
+                free(gx);
+            }
+            for (unsigned jr = 0; jr < nc; jr++) {
+                const unsigned nsx = ro[jr].nsx;
+                const double *e = est + (size_t)jr * per_ref;
+                for (unsigned ch = 0; ch < C; ch++)
+                    for (unsigned n = 0; n < nsx; n++) {
+                        unsigned px, py, pt;
+                        oc_coords(&c, ro[jr].idx[n], &px, &py, &pt);
+                        for (unsigned pp = 0; pp < k; pp++)
+                            for (unsigned q = 0; q < k; q++) {
+                                const size_t o = oc_index(&c, px + q, py + pp, pt, ch);
+                                const double kw = (double)(kai[pp * k + q] * ro[jr].w[ch]);
+                                num[o] += kw * e[(size_t)ch * nsx * k2 + (size_t)n * k2 + pp * k + q];
+                                den[o] += kw;
+                            }
+                    }
+            }
+        }
+    for (size_t i = 0; i < total; i++) out[i] = den[i] == 0 ? (step == 1 ? (double)x[i] : 0.0) : num[i] / den[i];
+    free(num);
+    free(den);
+    free(est);
+    free(ro);
+    free(rows);
+    free(cols);
+    return 0;
+}
+

@@ -52,6 +52,13 @@ int oracle_run(float sigma, float *noisy, const float *fflow, const float *bflow
 
 void oracle_color_transform(float *video, vbm3d_dims d, int forward);
 
+/* The frozen linearisation of one step (groups, masks / Wiener gains and
+ * weights from the forward pass on noisy / basic) applied to x, in double:
+ * the FP64 reference of vbm3d_linear_apply.  kt == 1 only. */
+int oracle_linear_apply(int step, const vbm3d_params *p, const float *noisy, const float *basic,
+                        const float *fflow, const float *bflow, vbm3d_dims d, float sigma, int color_space,
+                        const float *x, double *out, int threads);
+
 /* Transform kernels exposed for unit tests on one k x k block. */
 void oracle_dct2d_forward(const float *in, float *out, unsigned k);
 void oracle_dct2d_inverse(const float *in, float *out, unsigned k);

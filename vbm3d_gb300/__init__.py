@@ -55,6 +55,11 @@ def load(path=LIB_PATH):
     L.vbm3d_run_host.argtypes = [C.c_float, vp, vp, vp, vp, vp, P, P, C.c_int, Dims]
     L.vbm3d_gpu_similar_patches.argtypes = [P, vp, vp, vp, Dims, vp, vp, vp, vp, C.POINTER(C.c_size_t), vp]
     L.vbm3d_gpu_bm_distance_count.argtypes = [P, vp, vp, vp, Dims, C.POINTER(C.c_ulonglong), vp]
+    L.vbm3d_linear_create.argtypes = [C.c_int, P, vp, vp, vp, vp, Dims, C.c_float, C.c_int, C.POINTER(vp), vp]
+    L.vbm3d_linear_apply.argtypes = [vp, vp, vp, C.c_int, vp]
+    L.vbm3d_linear_den.argtypes = [vp, C.POINTER(vp)]
+    L.vbm3d_linear_destroy.argtypes = [vp]
+    L.vbm3d_linear_destroy.restype = None
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -169,6 +174,44 @@ def bm_distance_count(video, params, fflow=None, bflow=None, stream=None):
     _check(load().vbm3d_gpu_bm_distance_count(C.byref(params), _ptr(video), _ptr(fflow), _ptr(bflow), _dims(video),
                                               C.byref(n), _stream(stream)))
     return n.value
+
+
+class LinearStep:
+    """Frozen linearisation L of one step (vbm3d_linear_*): apply(x) = L x,
+    apply(x, adjoint=True) = L^T x.  Keeps references to its inputs."""
+
+    def __init__(self, step, noisy, sigma, params, basic=None, fflow=None, bflow=None, color_space=False,
+                 stream=None):
+        _video(noisy, "noisy")
+        self._keep = (noisy, basic, fflow, bflow)
+        self.shape = noisy.shape
+        self._h = C.c_void_p()
+        _check(load().vbm3d_linear_create(step, C.byref(params), _ptr(noisy), _ptr(basic), _ptr(fflow), _ptr(bflow),
+                                          _dims(noisy), sigma, int(color_space), C.byref(self._h), _stream(stream)))
+
+    def apply(self, x, adjoint=False, out=None, stream=None):
+        import torch
+        _video(x, "x")
+        out = torch.empty_like(x) if out is None else out
+        _check(load().vbm3d_linear_apply(self._h, _ptr(x), _ptr(out), int(adjoint), _stream(stream)))
+        return out
+
+    def den(self):
+        import torch
+        p = C.c_void_p()
+        _check(load().vbm3d_linear_den(self._h, C.byref(p)))
+        return p.value
+
+    def close(self):
+        if self._h:
+            load().vbm3d_linear_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=False, stream=None):

@@ -293,6 +293,11 @@ int build_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_spa
                 P.inv[j * k + u] = u == 0 ? 1.0f : (float)(2.0 * std::cos(pi * u * (j + 0.5) / k));  // REDFT01
             }
     }
+    for (unsigned i = 0; i < k; i++)
+        for (unsigned j = 0; j < k; j++) {
+            P.fwdT[i * k + j] = P.fwd[j * k + i];
+            P.invT[i * k + j] = P.inv[j * k + i];
+        }
     P.bm_warp_bytes = bm_warp_bytes(P, P.bm_list_cap, P.bm_best_cap, P.bm_win_cap);
     return VBM3D_OK;
 }

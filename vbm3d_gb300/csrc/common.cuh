@@ -62,6 +62,8 @@ struct StepParams {
     float inv[kMaxK * kMaxK];   // DCT: REDFT01 matrix [i][u]; bior: inverse basis rows
     float cn[kMaxK * kMaxK];    // DCT normalisation (preProcess, src/vbm3d.cpp:1843-1863)
     float cni[kMaxK * kMaxK];
+    float fwdT[kMaxK * kMaxK];  // transposes of fwd / inv (adjoint of the linearised filter)
+    float invT[kMaxK * kMaxK];
     // block-matching shared-memory layout (floats / pairs per warp)
     int bm_list_cap, bm_best_cap, bm_win_cap, bm_warp_bytes;
 };
