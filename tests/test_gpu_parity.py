@@ -187,6 +187,7 @@ def test_run_golden(dev, name):
     ((176, 144, 10, 1), 20.0, False, 1001),
     ((96, 80, 8, 3), 30.0, True, 1002),
     ((96, 80, 8, 3), 40.0, False, 1003),
+    ((50, 40, 5, 1), 50.0, True, 1004),   # colour flag on a one-channel clip: no transform
 ])
 def test_psnr_end_to_end(dev, oracle, shape, sigma, cs, seed):
     w, h, f, c = shape

@@ -552,7 +552,7 @@ int vbm3d_gpu_run(float sigma, float* noisy, const float* fflow, const float* bf
             goto out;
         }
     }
-    if (color_space) {
+    if (color_space && dims.channels == 3) {  // one-channel videos are left as they are
         launch_color(denoised, wh, dims.frames, 0, s);
         launch_color(noisy, wh, dims.frames, 0, s);
         cudaError_t e = launch_color(basic, wh, dims.frames, 0, s);
