@@ -208,6 +208,74 @@ int vbm3d_linear_apply(vbm3d_linear *state, const float *x, float *out, int adjo
 int vbm3d_linear_den(vbm3d_linear *state, const float **denominator);
 void vbm3d_linear_destroy(vbm3d_linear *state);
 
+/* Batched form, no reference counterpart (the reference denoises one clip
+ * per process run, src/main.cpp): many clips of uneven size, channel count
+ * and noise level denoised by one CUDA graph launch, each with
+ * vbm3d_gpu_run's semantics.  Unlike vbm3d_gpu_run, `noisy` is not
+ * modified; the outputs are written in RGB when colour_space is set.
+ *   vbm3d_batch_create: validates every clip, allocates the working buffers
+ *     (one cudaMalloc arena), builds the work queues, autotunes the phases
+ *     whose configuration is not given (one eager pass over the batch, on
+ *     the clips' current inputs), and captures the CUDA graph.  Synchronises
+ *     `stream` first, and the device before it returns.  The clips' device
+ *     pointers are baked into the graph: they must stay valid, and hold the
+ *     new inputs, for every vbm3d_batch_run.
+ *   vbm3d_batch_run: one graph launch on `stream` (stream-ordered).  Runs of
+ *     one batch share its working buffers: serialise them.
+ * Limits: both steps run (k > 0), k in {7, 8}, kt == 1, N <= 8, and the
+ * staged block-matching layout of the search windows fits 24 KB (true of
+ * the reference defaults for every sigma); other clips are rejected with
+ * VBM3D_ERR_UNSUPPORTED and run through vbm3d_gpu_run. */
+typedef struct vbm3d_clip {
+    vbm3d_dims dims;
+    float sigma;
+    const vbm3d_params *prms_1;  /* NULL: the reference defaults for sigma */
+    const vbm3d_params *prms_2;
+    const float *noisy;          /* device, W*H*F*C floats, read only */
+    const float *fflow;          /* device or NULL (zero flow) */
+    const float *bflow;
+    float *basic;                /* device output or NULL */
+    float *denoised;             /* device output */
+} vbm3d_clip;
+
+/* Per phase (block matching / filtering of each step): reference patches
+ * per work item and warps per block; 0 and 0 = autotune.  no_graph = 1
+ * enqueues the kernels at each run instead of launching the graph.  The
+ * last three fields are outputs of vbm3d_batch_get_config. */
+typedef struct vbm3d_batch_config {
+    int bm1_tile, bm1_warps;
+    int filter1_tile, filter1_warps;
+    int bm2_tile, bm2_warps;
+    int filter2_tile, filter2_warps;
+    int no_graph;
+    float tune_ms;               /* time spent in vbm3d_batch_create's tuning pass */
+    unsigned work_items;         /* items of the four work phases */
+    size_t device_bytes;         /* working arena */
+} vbm3d_batch_config;
+
+/* One work launch of a batch, as measured by vbm3d_batch_profile. */
+typedef struct vbm3d_batch_launch {
+    int phase;                   /* 0 / 2: block matching of step 1 / 2; 1 / 3: filtering */
+    int k, channels;             /* the launch's class (channels 0: any, for filtering) */
+    int clips;                   /* clips in the launch */
+    unsigned items;              /* work items */
+    unsigned long long refs;     /* reference patches */
+    int tile, warps, grid;       /* refs per item, warps per block, blocks */
+    float ms;                    /* CUDA-event duration */
+} vbm3d_batch_launch;
+
+typedef struct vbm3d_batch vbm3d_batch;
+int vbm3d_batch_create(const vbm3d_clip *clips, int nclips, int color_space,
+                       const vbm3d_batch_config *config, vbm3d_batch **batch, void *stream);
+int vbm3d_batch_run(vbm3d_batch *batch, void *stream);
+int vbm3d_batch_get_config(const vbm3d_batch *batch, vbm3d_batch_config *config);
+/* One run of the batch with its kernels enqueued one by one and a CUDA
+ * event around every work launch (same results as vbm3d_batch_run); fills
+ * out[0 .. *count) in launch order and synchronises `stream`.  Fails with
+ * VBM3D_ERR_INVALID_ARGUMENT, *count set, when cap < *count. */
+int vbm3d_batch_profile(vbm3d_batch *batch, void *stream, vbm3d_batch_launch *out, int cap, int *count);
+void vbm3d_batch_destroy(vbm3d_batch *batch);
+
 /* Measurement helper with no reference counterpart: runs the block
  * matching of vbm3d_gpu_similar_patches and returns in *count the total
  * number of patch distances it evaluated (calls of the reference's

@@ -116,3 +116,26 @@ def test_dropin_shim_compiles_against_reference_headers(tmp_path):
     syms = subprocess.check_output(["nm", "-C", str(tmp_path / "dropin.o")], text=True)
     for name in ("vbm3d_1st_step(", "vbm3d_2nd_step(", "run_vbm3d("):
         assert any(name in line and " T " in line for line in syms.splitlines()), name
+
+
+def test_batch_rejects_bad_clips_before_any_cuda_call(lib):
+    from vbm3d_gb300._abi import BatchConfig, Clip
+    fake = C.c_void_p(16)  # never dereferenced: validation fails first
+    h = C.c_void_p()
+    assert lib.vbm3d_batch_create(None, 0, 0, None, C.byref(h), None) == 1
+    p16 = vb.default_params(2, 20.0).replace(N=16)
+    clips = (Clip * 2)()
+    clips[0] = Clip(Dims(64, 48, 4, 3), 20.0, None, None, fake, None, None, None, fake)
+    clips[1] = Clip(Dims(64, 48, 4, 1), 20.0, None, C.pointer(p16), fake, None, None, None, fake)
+    assert lib.vbm3d_batch_create(clips, 2, 1, None, C.byref(h), None) == 2
+    assert b"clip 1 step 2" in lib.vbm3d_last_error()
+    clips[1] = Clip(Dims(64, 48, 4, 1), 20.0, None, None, None, None, None, None, fake)
+    assert lib.vbm3d_batch_create(clips, 2, 1, None, C.byref(h), None) == 1
+    clips[1] = Clip(Dims(64, 48, 4, 2), 20.0, None, None, fake, None, None, None, fake)
+    assert lib.vbm3d_batch_create(clips, 2, 1, None, C.byref(h), None) == 2
+    clips[1] = Clip(Dims(64, 48, 4, 1), 20.0, None, None, fake, None, None, None, fake)
+    bad = BatchConfig(bm1_tile=4, bm1_warps=3)
+    assert lib.vbm3d_batch_create(clips, 2, 1, C.byref(bad), C.byref(h), None) == 1
+    bad = BatchConfig(bm1_tile=4)
+    assert lib.vbm3d_batch_create(clips, 2, 1, C.byref(bad), C.byref(h), None) == 1
+    assert not h.value

@@ -13,11 +13,15 @@ Entry points mirror the reference's hot path (tehret/vbm3d):
   color_transform(...)               VideoUtils::transformColorSpace
   similar_patches(...)               computeSimilarPatches over the reference grid
   run(...) / run_host(...)           run_vbm3d (src/vbm3d.cpp:87-376), device / host buffers
+Beside them, with no reference counterpart:
+  Batch(...)                         many uneven clips in one CUDA graph (vbm3d_batch_*)
+  LinearStep(...)                    frozen linearisation and adjoint of a step (vbm3d_linear_*)
 """
 import ctypes as C
 import os
 
-from ._abi import BIOR, DCT, HAAR, HADAMARD, STATUS, Dims, Params, dims_of  # noqa: F401
+from ._abi import (BIOR, DCT, HAAR, HADAMARD, STATUS, BatchConfig, BatchLaunch, Clip, Dims,  # noqa: F401
+                   Params, dims_of)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libvbm3d_gb300.so")
@@ -60,6 +64,12 @@ def load(path=LIB_PATH):
     L.vbm3d_linear_den.argtypes = [vp, C.POINTER(vp)]
     L.vbm3d_linear_destroy.argtypes = [vp]
     L.vbm3d_linear_destroy.restype = None
+    L.vbm3d_batch_create.argtypes = [C.POINTER(Clip), C.c_int, C.c_int, C.POINTER(BatchConfig), C.POINTER(vp), vp]
+    L.vbm3d_batch_run.argtypes = [vp, vp]
+    L.vbm3d_batch_get_config.argtypes = [vp, C.POINTER(BatchConfig)]
+    L.vbm3d_batch_profile.argtypes = [vp, vp, C.POINTER(BatchLaunch), C.c_int, C.POINTER(C.c_int)]
+    L.vbm3d_batch_destroy.argtypes = [vp]
+    L.vbm3d_batch_destroy.restype = None
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -205,6 +215,69 @@ class LinearStep:
     def close(self):
         if self._h:
             load().vbm3d_linear_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many clips of uneven size, channel count and sigma denoised by one CUDA
+    graph launch (vbm3d_batch_*).  `clips` is a list of dicts with keys
+    noisy (CUDA float32 [F, C, H, W]), sigma, and optionally fflow, bflow,
+    p1, p2.  Outputs are allocated here: self.basic[i] (None when basic is
+    False), self.denoised[i].  `config` (a BatchConfig or a dict of its
+    fields) fixes phases instead of autotuning them.  The inputs are kept
+    referenced; refill them in place between runs."""
+
+    def __init__(self, clips, color_space=False, config=None, basic=True, stream=None):
+        import torch
+        self._keep = []
+        self.basic, self.denoised = [], []
+        arr = (Clip * len(clips))()
+        for i, c in enumerate(clips):
+            noisy = _video(c["noisy"], "noisy")
+            sigma = float(c["sigma"])
+            p1 = c.get("p1") or default_params(1, sigma)
+            p2 = c.get("p2") or default_params(2, sigma)
+            den = torch.empty_like(noisy)
+            bas = torch.empty_like(noisy) if basic else None
+            self.basic.append(bas)
+            self.denoised.append(den)
+            self._keep += [noisy, c.get("fflow"), c.get("bflow"), p1, p2]
+            arr[i] = Clip(_dims(noisy), sigma, C.pointer(p1), C.pointer(p2), _ptr(noisy), _ptr(c.get("fflow")),
+                          _ptr(c.get("bflow")), _ptr(bas), _ptr(den))
+        self._clips = arr
+        cfg = None
+        if config is not None:
+            cfg = config if isinstance(config, BatchConfig) else BatchConfig(**config)
+        self._h = C.c_void_p()
+        _check(load().vbm3d_batch_create(arr, len(clips), int(color_space), None if cfg is None else C.byref(cfg),
+                                         C.byref(self._h), _stream(stream)))
+
+    def run(self, stream=None):
+        _check(load().vbm3d_batch_run(self._h, _stream(stream)))
+        return self.basic, self.denoised
+
+    def profile(self, stream=None):
+        """One run with a CUDA event around each work launch: a list of dicts
+        (phase, k, channels, clips, items, refs, tile, warps, grid, ms)."""
+        n = C.c_int(0)
+        buf = (BatchLaunch * 64)()
+        _check(load().vbm3d_batch_profile(self._h, _stream(stream), buf, 64, C.byref(n)))
+        return [buf[i].as_dict() for i in range(n.value)]
+
+    def config(self):
+        c = BatchConfig()
+        _check(load().vbm3d_batch_get_config(self._h, C.byref(c)))
+        return c.as_dict()
+
+    def close(self):
+        if self._h:
+            load().vbm3d_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

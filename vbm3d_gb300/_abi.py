@@ -54,3 +54,35 @@ def dims_of(video):
     """Dims of a [F, C, H, W] array."""
     f, c, h, w = video.shape
     return Dims(w, h, f, c)
+
+
+class Clip(C.Structure):
+    """vbm3d_clip: one clip of a batch (device pointers)."""
+    _fields_ = [("dims", Dims), ("sigma", C.c_float),
+                ("prms_1", C.POINTER(Params)), ("prms_2", C.POINTER(Params)),
+                ("noisy", C.c_void_p), ("fflow", C.c_void_p), ("bflow", C.c_void_p),
+                ("basic", C.c_void_p), ("denoised", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    """vbm3d_batch_config: refs per work item and warps per block of each
+    phase (0, 0 = autotune), the graph switch, and three outputs."""
+    _fields_ = [("bm1_tile", C.c_int), ("bm1_warps", C.c_int),
+                ("filter1_tile", C.c_int), ("filter1_warps", C.c_int),
+                ("bm2_tile", C.c_int), ("bm2_warps", C.c_int),
+                ("filter2_tile", C.c_int), ("filter2_warps", C.c_int),
+                ("no_graph", C.c_int), ("tune_ms", C.c_float),
+                ("work_items", C.c_uint), ("device_bytes", C.c_size_t)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class BatchLaunch(C.Structure):
+    """vbm3d_batch_launch: one work launch measured by vbm3d_batch_profile."""
+    _fields_ = [("phase", C.c_int), ("k", C.c_int), ("channels", C.c_int), ("clips", C.c_int),
+                ("items", C.c_uint), ("refs", C.c_ulonglong), ("tile", C.c_int), ("warps", C.c_int),
+                ("grid", C.c_int), ("ms", C.c_float)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

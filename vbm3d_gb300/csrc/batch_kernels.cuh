@@ -1,0 +1,117 @@
+// Work kernels of the batched form (persistent, queue-driven); included by
+// batch_step1.cu and batch_step2.cu, which instantiate them.
+#pragma once
+
+#include "batch.cuh"
+#include "filter_common.cuh"
+
+namespace vbm3d {
+namespace batched {
+
+// Block-wide word copy (a clip's parameters into shared memory).
+__device__ __forceinline__ void copy_words(void* dst, const void* src, int bytes)
+{
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = __ldg(s + i);
+}
+
+constexpr unsigned kNoItem = 0xffffffffu;
+
+// Work items are taken one ahead: thread 0 claims the block's next item
+// (one atomicAdd on the queue head) while the block works on the current
+// one, and the barrier that ends the current item publishes it, so a block
+// waits at one barrier per item and never for the queue.
+__device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsigned nitems, unsigned* head,
+                                           uint4* slot)
+{
+    if (threadIdx.x == 0) {
+        const unsigned it = atomicAdd(head, 1u);
+        *slot = it < nitems ? items[it] : make_uint4(kNoItem, 0u, 0u, 0u);
+    }
+}
+
+// ------------------------------------------------------- work phases ---
+// One kernel per class (K, C) of block matching and per table set of
+// filtering, as the plain path has, so each holds one copy of the
+// per-reference body.  A work item is taken by a whole block; its warps
+// handle interleaved references of the tile (warp w: references w,
+// w + warps, ...), so at any time a block works on neighbouring reference
+// patches whose search windows and groups overlap in L1, as a block of the
+// plain kernel does.  A block keeps its current clip's parameters in
+// shared memory, reloaded when an item of another clip comes up.
+
+template <int STEP, int K, int C>
+__global__ void __maxnreg__(C == 3 ? 96 : 80)  // as bm2_kernel
+batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
+                unsigned* __restrict__ head, int warp_bytes)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint4 s_item[2];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    StepHead* P = reinterpret_cast<StepHead*>(smem);
+    Layout* L = reinterpret_cast<Layout*>(smem + kHeadBytes);
+    unsigned char* ws = smem + kHeadBytes + kLayoutBytes + (size_t)wid * warp_bytes;
+    unsigned cur = kNoItem;
+    claim_item(items, nitems, head, &s_item[0]);
+    __syncthreads();
+    for (int buf = 0;; buf ^= 1) {
+        const uint4 I = s_item[buf];
+        if (I.x == kNoItem) break;
+        claim_item(items, nitems, head, &s_item[buf ^ 1]);
+        const BatchClip& B = clips[I.x];
+        if (I.x != cur) {  // uniform over the block
+            copy_words(P, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
+            copy_words(L, &B.s[STEP - 1].L, (int)sizeof(Layout));
+            __syncthreads();
+            cur = I.x;
+        }
+        const float* vid = STEP == 1 ? B.y : B.basic;
+        for (unsigned j = wid; j < I.z; j += nwarps) {
+            // register copies: the fields bm2_ref reads are loaded once per
+            // reference, not reloaded after each of its shared-memory stores
+            const StepHead Pr = *P;
+            const Layout Lr = *L;
+            bm2_ref<K, C>(Pr, Lr, (long long)I.y + j, ws, lane, vid, B.fflow, B.bflow, B.tab_idx, nullptr, nullptr,
+                          B.tab_nsx);
+            __syncwarp();
+        }
+        __syncthreads();  // publishes the next item; the parameters are reused
+    }
+}
+
+template <int STEP, int K>
+__global__ void __launch_bounds__(256, 2)
+batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
+                    unsigned* __restrict__ head, int warp_floats)
+{
+    extern __shared__ __align__(16) float fsm[];
+    __shared__ uint4 s_item[2];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    FilterView* V = reinterpret_cast<FilterView*>(fsm);
+    float* base = fsm + kViewFloats + (size_t)wid * warp_floats;
+    unsigned cur = kNoItem;
+    claim_item(items, nitems, head, &s_item[0]);
+    __syncthreads();
+    for (int buf = 0;; buf ^= 1) {
+        const uint4 I = s_item[buf];
+        if (I.x == kNoItem) break;
+        claim_item(items, nitems, head, &s_item[buf ^ 1]);
+        const BatchClip& B = clips[I.x];
+        if (I.x != cur) {
+            copy_words(V, &B.s[STEP - 1].v, (int)sizeof(FilterView));
+            __syncthreads();
+            cur = I.x;
+        }
+        const AggTarget A{nullptr, nullptr, B.pair};
+        for (unsigned j = wid; j < I.z; j += nwarps) {
+            filter_ref<STEP, K, true>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                      B.tab_nsx, A);
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace batched
+}  // namespace vbm3d

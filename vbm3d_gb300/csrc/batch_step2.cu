@@ -1,0 +1,31 @@
+// Step-2 work kernels of the batched form (see batch.cu), one translation
+// unit per step so that the two compile in parallel.
+#include "batch_kernels.cuh"
+
+namespace vbm3d {
+namespace batched {
+
+const void* work_kernel_step2(int phase, int cls)
+{
+    if (phase == 2) {
+        switch (cls) {
+            case 0: return reinterpret_cast<const void*>(batch_bm_kernel<2, 7, 1>);
+            case 1: return reinterpret_cast<const void*>(batch_bm_kernel<2, 7, 3>);
+            case 2: return reinterpret_cast<const void*>(batch_bm_kernel<2, 8, 1>);
+            case 3: return reinterpret_cast<const void*>(batch_bm_kernel<2, 8, 3>);
+            default: return nullptr;
+        }
+    }
+    if (phase == 3) {
+        switch (cls) {
+            case 0: return reinterpret_cast<const void*>(batch_filter_kernel<2, 7>);
+            case 1:  // DCT and bior1.5 tables share the k = 8 kernel
+            case 2: return reinterpret_cast<const void*>(batch_filter_kernel<2, 8>);
+            default: return nullptr;
+        }
+    }
+    return nullptr;
+}
+
+}  // namespace batched
+}  // namespace vbm3d

@@ -1,0 +1,620 @@
+// Staged block matching (see bm2.cu): device code shared by the
+// single-video kernel (bm2.cu) and the batched persistent kernels
+// (batch_kernels.cuh).
+#pragma once
+
+#include "common.cuh"
+
+namespace vbm3d {
+
+// Shared-memory layout of one warp of the staged kernel (bm2_layout).
+struct Layout {
+    int warp_bytes;   // shared memory per warp
+    int tile_floats;  // staged windows
+    int res_cap;      // distances of a phase / the final list
+    int scr_cap;      // tie fallback scratch (one window)
+};
+
+namespace {
+
+
+struct Win {
+    int t, x0, x1, y0, y1;
+};
+
+// A window of the current phase.
+struct PWin {
+    int t, x0, y0, ww, wh;  // clamped window: positions x0..x0+ww-1, y0..y0+wh-1
+    int tile;               // float offset of its staged tile
+    int res;                // offset of its results in the phase result array
+    int chain;              // 0: reference frame, 1: forward, 2: backward
+    float rcp_ww;           // 1 / ww, to split positions into (row, column)
+    unsigned long long seen;  // earlier windows on the same frame (bit i: scanned window i)
+};
+
+static_assert(sizeof(PWin) % 16 == 0, "phase windows stay 8-byte aligned in shared memory");
+
+// Inside the kernel a patch is named by packed coordinates
+// ((t - rt + 32) << 26) | (y << 13) | x (x, y < 8192, |t - rt| <= 16),
+// which decode without divisions; the output converts them to the
+// reference's linear indices.
+__device__ __forceinline__ unsigned pack_xyt(int x, int y, int t, int rt)
+{
+    return ((unsigned)(t - rt + 32) << 26) | ((unsigned)y << 13) | (unsigned)x;
+}
+__device__ __forceinline__ void unpack_xyt(unsigned v, int rt, int& x, int& y, int& t)
+{
+    x = (int)(v & 8191u);
+    y = (int)((v >> 13) & 8191u);
+    t = (int)(v >> 26) - 32 + rt;
+}
+
+// Row of position j in a window of width ww (exact: j < 2^8, ww <= 15).
+__device__ __forceinline__ int pos_row(int j, float rcp_ww) { return (int)(((float)j + 0.5f) * rcp_ww); }
+
+constexpr unsigned kNone = 0xffffffffu;
+
+// Row pitch (and height) of a staged window tile of side s + k - 1: at
+// least 13 and odd, which keeps the rows of a 5-wide window on distinct
+// shared-memory banks.
+__host__ __device__ __forceinline__ int bm2_pitch(int s, int k)
+{
+    const int p = s + k - 1;
+    return p <= 13 ? 13 : (p | 1);
+}
+
+// (a, b) += ((r, r) - (xa, xb))^2 with the rounding of the scalar
+// sequence d = r - x; s = s + d * d.  The subtraction and the accumulation
+// are packed f32x2 operations; the squares stay scalar multiplies, because
+// a packed multiply followed by a packed add is contracted into a fused
+// multiply-add below the PTX level (a GB300 probe found that pairing
+// changes the result in about half of all 192-term sums), whereas this
+// form reproduces the scalar sums bit for bit.
+__device__ __forceinline__ void sq_acc2(float& ax, float& ay, float rx, float ry, float xa, float xb)
+{
+    float dx, dy;
+    asm("{\n\t.reg .b64 r, x, d;\n\t"
+        "mov.b64 r, {%2, %3};\n\t"
+        "mov.b64 x, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, r, x;\n\t"
+        "mov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(dx), "=f"(dy)
+        : "f"(rx), "f"(ry), "f"(xa), "f"(xb));
+    dx = __fmul_rn(dx, dx);
+    dy = __fmul_rn(dy, dy);
+    asm("{\n\t.reg .b64 a, d;\n\t"
+        "mov.b64 a, {%0, %1};\n\t"
+        "mov.b64 d, {%2, %3};\n\t"
+        "add.rn.f32x2 a, a, d;\n\t"
+        "mov.b64 {%0, %1}, a;\n\t}"
+        : "+f"(ax), "+f"(ay)
+        : "f"(dx), "f"(dy));
+}
+
+struct Smem {
+    Pair* scr;     // tie fallback scratch
+    float2* refp;  // C*k*k duplicated reference pixels
+    float* tiles;  // staged windows of the phase
+    Win* wins;     // every window scanned so far
+    PWin* pw;      // windows of the current phase
+    Pair* res;     // distances of the phase, per window in scan order (i == kNone: not a candidate)
+    Pair* fc;      // [2][Nb*Nb] frame candidates of the forward / backward step
+    Pair* best;    // [Nb | Nb*Nf forward | Nb*Nf backward]
+    unsigned* cen; // [2][Nb] forward / backward centres (tempMatchesPost / Pre)
+    int* cnt;      // per-chain counters
+};
+
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Number of positions of a window.
+__device__ __forceinline__ int npos(const PWin& w) { return w.ww * w.wh; }
+
+// Top-min(Nb, #valid) of window w (distances in S.res[w.res ...], scan
+// order), appended sorted to out[*nout]: localSearch's partial_sort
+// (src/vbm3d.cpp:1075-1079).
+__device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, int lane, Pair* out, int& nout,
+                              Pair* scratch)
+{
+    const int n = npos(w);
+    const Pair* res = S.res + w.res;
+    int nvalid = 0;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        const int j = j0 + lane;
+        nvalid += __popc(__ballot_sync(kFull, j < n && res[j].i != kNone));
+    }
+    const int m = min(P.Nb, nvalid);
+    bool tie = false;
+    // fast path: exact ranks of the m smallest
+    float last = -__int_as_float(0x7f800000);
+    for (int r = 0; r < m; r++) {
+        // smallest distance strictly above `last`
+        float lmin = __int_as_float(0x7f800000);
+        int lj = -1, lcnt = 0;
+        for (int j = lane; j < n; j += 32) {
+            const Pair e = res[j];
+            if (e.i == kNone || !(e.d > last)) continue;
+            if (lj < 0 || e.d < lmin) {
+                lmin = e.d;
+                lj = j;
+                lcnt = 1;
+            } else if (e.d == lmin) {
+                lcnt++;
+            }
+        }
+        float wmin = lmin;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) wmin = fminf(wmin, __shfl_xor_sync(kFull, wmin, off));
+        const int c = (lj >= 0 && lmin == wmin) ? lcnt : 0;
+        const int tot = __reduce_add_sync(kFull, c);
+        if (tot != 1) {
+            tie = true;
+            break;
+        }
+        const unsigned bal = __ballot_sync(kFull, c == 1);
+        const int wl = __ffs(bal) - 1;
+        const int wj = __shfl_sync(kFull, lj, wl);
+        if (lane == 0) out[nout + r] = res[wj];
+        last = wmin;
+    }
+    if (tie) {
+        __syncwarp();
+        if (lane == 0) {
+            int k = 0;
+            for (int j = 0; j < n; j++)
+                if (res[j].i != kNone) scratch[k++] = res[j];
+            partial_sort(scratch, m, k);
+            for (int r = 0; r < m; r++) out[nout + r] = scratch[r];
+        }
+    }
+    nout += m;
+    __syncwarp();
+}
+
+// Sorted smallest `m` of a[0..n) written to out (std::partial_sort order):
+// exact ranks when all keys of the prefix are distinct, else the
+// restatement of the reference's routine on one lane.
+__device__ void small_partial_sort(Pair* a, int m, int n, int lane)
+{
+    if (n > 32) {
+        if (lane == 0) partial_sort(a, m, n);
+        __syncwarp();
+        return;
+    }
+    bool ok = true;
+    int rank = 0;
+    Pair mine = {0.f, 0};
+    if (lane < n) {
+        mine = a[lane];
+        for (int j = 0; j < n; j++) {
+            const float d = a[j].d;
+            if (d < mine.d) rank++;
+            else if (d == mine.d && j != lane) ok = false;
+        }
+    }
+    // ties among entries that cannot reach the prefix do not matter, but
+    // keep it simple: any tie sends the list to the exact routine
+    ok = __all_sync(kFull, ok);
+    __syncwarp();
+    if (ok) {
+        if (lane < n && rank < m) a[rank] = mine;  // ranks are distinct: a permutation of the prefix
+    } else if (lane == 0) {
+        partial_sort(a, m, n);
+    }
+    __syncwarp();
+}
+
+template <int K, int C>
+__device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
+                                int pitch, int plane)
+{
+    constexpr int KK = K * K;
+    // pair windows (0,1), (2,3), ...; an odd last window is split in
+    // halves.  Each pair owns whole 32-lane rows of slots (slot j of a pair
+    // = position j of both windows), so one load instruction reads one tile
+    // and the rows of a window fall on distinct banks.
+    const int npairs = (nw + 1) / 2;
+    int rows_before[kMaxNb + 1];
+    int nrows = 0;
+#pragma unroll
+    for (int p = 0; p < kMaxNb; p++) {
+        rows_before[p] = nrows;
+        if (p < npairs) {
+            const int wa = 2 * p, wb = 2 * p + 1;
+            const int na = npos(S.pw[wa]);
+            const int slots = wb < nw ? max(na, npos(S.pw[wb])) : (na + 1) / 2;
+            nrows += (slots + 31) >> 5;
+        }
+    }
+    rows_before[kMaxNb] = nrows;
+
+    for (int rb = 0; rb < nrows; rb += 2) {
+        // two slot rows per pass; each slot carries two candidates
+        const float* tp[4];
+        int rslot[4], qxy[4], win[4];
+        bool valid[4];
+#pragma unroll
+        for (int s2 = 0; s2 < 2; s2++) {
+            const int row = rb + s2;
+            int p = 0;
+#pragma unroll
+            for (int q = 1; q < kMaxNb; q++) p += (row >= rows_before[q] && q < npairs) ? 1 : 0;
+            const int j = ((row - rows_before[p]) << 5) + lane;
+            const int wa = 2 * p, wb = 2 * p + 1;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c4 = 2 * s2 + h;
+                valid[c4] = false;
+                tp[c4] = S.tiles;
+                win[c4] = 0;
+                rslot[c4] = 0;
+                qxy[c4] = 0;
+                if (row >= nrows) continue;
+                int w = wa, pos = j;
+                if (wb < nw) {
+                    w = h ? wb : wa;
+                } else {
+                    const int half = (npos(S.pw[wa]) + 1) / 2;
+                    if (j >= half) continue;
+                    if (h) pos = j + half;
+                }
+                const PWin pwn = S.pw[w];
+                if (pos < npos(pwn)) {
+                    const int dy = pos_row(pos, pwn.rcp_ww), dx = pos - dy * pwn.ww;
+                    valid[c4] = true;
+                    tp[c4] = S.tiles + pwn.tile + dy * pitch + dx;
+                    win[c4] = w;
+                    rslot[c4] = pwn.res + pos;
+                    qxy[c4] = ((pwn.y0 + dy) << 16) | (pwn.x0 + dx);
+                }
+            }
+        }
+        const bool two = __any_sync(kFull, valid[2] || valid[3]);
+        float a0x = 0.f, a0y = 0.f, a1x = 0.f, a1y = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < C; c++) {
+            const float* t0 = tp[0] + c * plane;
+            const float* t1 = tp[1] + c * plane;
+            const float2* rr = S.refp + c * KK;
+            if (two) {
+                const float* t2 = tp[2] + c * plane;
+                const float* t3 = tp[3] + c * plane;
+#pragma unroll 1
+                for (int hy = 0; hy < K; hy++)
+#pragma unroll
+                    for (int hx = 0; hx < K; hx++) {
+                        const float2 r2 = rr[hy * K + hx];
+                        sq_acc2(a0x, a0y, r2.x, r2.y, t0[hy * pitch + hx], t1[hy * pitch + hx]);
+                        sq_acc2(a1x, a1y, r2.x, r2.y, t2[hy * pitch + hx], t3[hy * pitch + hx]);
+                    }
+            } else {
+#pragma unroll 1
+                for (int hy = 0; hy < K; hy++)
+#pragma unroll
+                    for (int hx = 0; hx < K; hx++) {
+                        const float2 r2 = rr[hy * K + hx];
+                        sq_acc2(a0x, a0y, r2.x, r2.y, t0[hy * pitch + hx], t1[hy * pitch + hx]);
+                    }
+            }
+        }
+        const float acc[4] = {a0x, a0y, a1x, a1y};
+        const float norm = (float)(KK * C);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (!valid[q]) continue;
+            const PWin& pwn = S.pw[win[q]];
+            const int qx = qxy[q] & 0xffff, qy = qxy[q] >> 16;
+            // seen: inside an earlier window on the same frame
+            bool seen = false;
+            unsigned long long m = pwn.seen;
+            while (m) {
+                const int wi = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                const Win v = S.wins[wi];
+                if (qx >= v.x0 && qx <= v.x1 && qy >= v.y0 && qy <= v.y1) {
+                    seen = true;
+                    break;
+                }
+            }
+            Pair e;
+            e.i = kNone;
+            e.d = 0.f;
+            if (!seen) {
+                float d = acc[q] / norm;
+                if (qx == rx && qy == ry) d = d - P.dbias;
+                e.d = d;
+                e.i = pack_xyt(qx, qy, pwn.t, rt);
+            }
+            S.res[rslot[q]] = e;
+        }
+    }
+    __syncwarp();
+}
+
+// Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
+// channels, at tile pitch `pitch`.
+// 4-byte asynchronous global -> shared copy (no register round trip).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+
+template <int K, int C>
+__device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, int lane,
+                            int pitch, int plane)
+{
+    // every tile row of every window is copied asynchronously, then waited
+    // for once: the loads of the whole phase are in flight together
+    for (int w = 0; w < nw; w++) {
+        const PWin pwn = S.pw[w];
+        const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
+        const float* src = vid + (size_t)pwn.t * P.whc + (size_t)pwn.y0 * P.W + pwn.x0;
+        float* dst = S.tiles + pwn.tile;
+        const int x = tw <= 16 ? (lane & 15) : lane, ystep = tw <= 16 ? 2 : 1, y0 = tw <= 16 ? (lane >> 4) : 0;
+        if (x < tw) {
+#pragma unroll 1
+            for (int c = 0; c < C; c++) {
+                const float* sc = src + (size_t)c * P.wh + x;
+                float* dc = dst + c * plane + x;
+#pragma unroll 4
+                for (int y = y0; y < th; y += ystep) cp_async4(dc + y * pitch, sc + (size_t)y * P.W);
+            }
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+}
+
+// Registers the phase's windows in the list of scanned windows (after the
+// phase's seen masks were computed against the earlier ones).
+__device__ void register_windows(const Smem& S, int nw, int lane)
+{
+    const int n0 = S.cnt[2];
+    if (lane < nw) {
+        const PWin pwn = S.pw[lane];
+        S.wins[n0 + lane] = Win{pwn.t, pwn.x0, pwn.x0 + pwn.ww - 1, pwn.y0, pwn.y0 + pwn.wh - 1};
+    }
+    __syncwarp();
+    if (lane == 0) S.cnt[2] = n0 + nw;
+    __syncwarp();
+}
+
+// The clamped window of side s around (cx, cy) (src/vbm3d.cpp:1045-1053).
+__device__ __forceinline__ PWin make_window(const StepHead& P, int t, int cx, int cy, int s, int chain)
+{
+    const int half = (s - 1) / 2;
+    const int x0 = max(0, cx - half), y0 = max(0, cy - half);
+    const int x1 = min(P.W - P.k, cx + half), y1 = min(P.H - P.k, cy + half);
+    PWin w;
+    w.t = t;
+    w.x0 = x0;
+    w.y0 = y0;
+    w.ww = x1 - x0 + 1;
+    w.wh = y1 - y0 + 1;
+    w.chain = chain;
+    w.tile = 0;
+    w.res = 0;
+    w.rcp_ww = 1.0f / (float)w.ww;
+    w.seen = 0ull;
+    return w;
+}
+
+// Block matching of reference patch r by one warp (lane 0..31), with the
+// warp's shared-memory region ws laid out by L.
+template <int K, int C>
+__device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long long r, unsigned char* ws, int lane,
+                                        const float* __restrict__ vid, const float* __restrict__ fflow,
+                                        const float* __restrict__ bflow, unsigned* __restrict__ out_idx,
+                                        float* __restrict__ out_dist, unsigned* __restrict__ out_nsimp,
+                                        unsigned* __restrict__ out_nsx)
+{
+    constexpr int KK = K * K;
+    const int Nb = P.Nb;
+    Smem S;
+    size_t off = 0;
+    S.refp = reinterpret_cast<float2*>(ws + off);
+    off = align16(off + sizeof(float2) * C * KK);
+    S.tiles = reinterpret_cast<float*>(ws + off);
+    off = align16(off + sizeof(float) * L.tile_floats);
+    S.res = reinterpret_cast<Pair*>(ws + off);
+    off = align16(off + sizeof(Pair) * L.res_cap);
+    S.scr = reinterpret_cast<Pair*>(ws + off);
+    off = align16(off + sizeof(Pair) * L.scr_cap);
+    S.fc = reinterpret_cast<Pair*>(ws + off);
+    off = align16(off + sizeof(Pair) * 2 * Nb * Nb);
+    S.best = reinterpret_cast<Pair*>(ws + off);
+    off = align16(off + sizeof(Pair) * P.bm_best_cap);
+    S.wins = reinterpret_cast<Win*>(ws + off);
+    off = align16(off + sizeof(Win) * P.bm_win_cap);
+    S.pw = reinterpret_cast<PWin*>(ws + off);
+    off = align16(off + sizeof(PWin) * 2 * Nb);
+    S.cen = reinterpret_cast<unsigned*>(ws + off);
+    off = align16(off + sizeof(unsigned) * 2 * kMaxNb);
+    S.cnt = reinterpret_cast<int*>(ws + off);  // [0..2]: counters, [3..]: windows before phase window w
+
+    int rx, ry, rt;
+    ref_coords(P, r, rx, ry, rt);
+    for (int e = lane; e < C * KK; e += 32) {
+        const int c = e / KK, pq = e - c * KK, py = pq / K, px = pq - py * K;
+        const float v = __ldg(vid + (size_t)rt * P.whc + (size_t)c * P.wh + (size_t)(ry + py) * P.W + rx + px);
+        S.refp[e] = make_float2(v, v);
+    }
+    if (lane == 0) {
+        S.cnt[2] = 0;  // windows scanned
+    }
+    __syncwarp();
+
+    // ---- phase 0: the reference frame (src/vbm3d.cpp:1114-1119)
+    {
+        const int pitch = bm2_pitch(P.Ns, K), plane = pitch * (P.Ns + K - 1);
+        if (lane == 0) {
+            PWin w = make_window(P, rt, rx, ry, P.Ns, 0);
+            S.pw[0] = w;
+            S.cnt[3] = 0;
+        }
+        __syncwarp();
+        stage_tiles<K, C>(P, S, vid, 1, lane, pitch, plane);
+        phase_distances<K, C>(P, S, 1, lane, rx, ry, rt, pitch, plane);
+        register_windows(S, 1, lane);
+        int n0 = 0;
+        select_window(P, S, S.pw[0], lane, S.best, n0, S.scr);
+        if (lane < Nb) {
+            // the reference reads Nb entries here (src/vbm3d.cpp:1115-1119);
+            // the host rejects grids whose corner window holds fewer
+            S.cen[lane] = S.best[lane].i;          // forward chain centres
+            S.cen[kMaxNb + lane] = S.best[lane].i; // backward chain centres
+        }
+        __syncwarp();
+    }
+
+    const int fend = min(rt + P.Nf, P.F - P.kt) - rt;
+    const int bend = min(rt, P.Nf);
+    const int nphase = max(fend, bend);
+    int nbf = 0, nbb = 0;  // picks of the forward / backward chains so far
+    Pair* bestf = S.best + Nb;
+    Pair* bestb = S.best + Nb + Nb * P.Nf;
+    const int pitch = bm2_pitch(P.Npr, K), plane = pitch * (P.Npr + K - 1);
+    const int tile_sz = C * plane;
+    for (int f = 1; f <= nphase; f++) {
+        // windows of this phase, one per lane: forward step f
+        // (src/vbm3d.cpp:1126-1133), then backward step f (:1150-1157)
+        const bool fa = f <= fend, ba = f <= bend;
+        const int nw = (fa ? Nb : 0) + (ba ? Nb : 0);
+        {
+            PWin w;
+            int n = 0;
+            if (lane < nw) {
+                const int chain = (fa && lane < Nb) ? 1 : 2;
+                const int m = chain == 1 ? lane : lane - (fa ? Nb : 0);
+                int px, py, pt;
+                unpack_xyt(S.cen[(chain - 1) * kMaxNb + m], rt, px, py, pt);
+                const float* flow = chain == 1 ? fflow : bflow;
+                const int ft = chain == 1 ? pt : pt - 1;  // fflow(.., pt) / bflow(.., pt - 1)
+                const float* fl = flow ? flow + (size_t)ft * 2 * P.wh : nullptr;
+                const float fx = fl ? __ldg(fl + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
+                px = min(max((int)((float)px + roundf(fx)), 0), P.W - K);
+                const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
+                py = min(max((int)((float)py + roundf(fy)), 0), P.H - K);
+                w = make_window(P, chain == 1 ? pt + 1 : pt - 1, px, py, P.Npr, chain);
+                w.tile = lane * tile_sz;
+                n = npos(w);
+            }
+            // exclusive prefix sum of the window sizes: result offsets
+            int incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane < nw) {
+                w.res = incl - n;
+                S.pw[lane] = w;
+                S.cnt[3 + lane] = S.cnt[2] + lane;  // earlier windows: all registered + earlier in this phase
+            }
+            __syncwarp();
+        }
+        // this phase's windows must be visible to the seen test of later
+        // windows of the same phase: register them first, then test each
+        // window against the windows registered before it (S.cnt[3 + w])
+        register_windows(S, nw, lane);
+        // seen masks: windows registered before each one, on its frame
+        for (int w = 0; w < nw; w++) {
+            const int lim = S.cnt[3 + w], wt = S.pw[w].t;
+            const unsigned lo = __ballot_sync(kFull, lane < lim && S.wins[lane].t == wt);
+            const unsigned hi = __ballot_sync(kFull, lane + 32 < lim && S.wins[lane + 32].t == wt);
+            if (lane == 0) S.pw[w].seen = ((unsigned long long)hi << 32) | lo;
+        }
+        __syncwarp();
+        stage_tiles<K, C>(P, S, vid, nw, lane, pitch, plane);
+        phase_distances<K, C>(P, S, nw, lane, rx, ry, rt, pitch, plane);
+
+        // per chain: top-Nb of each window, then of their union
+        int w0 = 0;
+        for (int chain = 1; chain <= 2; chain++) {
+            if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
+            Pair* fc = S.fc + (chain - 1) * Nb * Nb;
+            int nfc = 0;
+            for (int m = 0; m < Nb; m++) select_window(P, S, S.pw[w0 + m], lane, fc, nfc, S.scr);
+            w0 += Nb;
+            const int m2 = min(Nb, nfc);
+            small_partial_sort(fc, m2, nfc, lane);
+            Pair* dst = chain == 1 ? bestf + nbf : bestb + nbb;
+            if (lane < m2) {
+                S.cen[(chain - 1) * kMaxNb + lane] = fc[lane].i;
+                dst[lane] = fc[lane];
+            }
+            if (chain == 1) nbf += m2;
+            else nbb += m2;
+            __syncwarp();
+        }
+    }
+
+    // final selection (src/vbm3d.cpp:1169-1184): frame-t picks, forward picks,
+    // backward picks, in that order
+    Pair* lst = S.res;
+    const int nb0 = Nb;  // frame-t picks: exactly Nb (the host validates the corner window)
+    const int nbest = nb0 + nbf + nbb;
+    for (int j = lane; j < nbest; j += 32) {
+        Pair e;
+        if (j < nb0) e = S.best[j];
+        else if (j < nb0 + nbf) e = bestf[j - nb0];
+        else e = bestb[j - nb0 - nbf];
+        lst[j] = e;
+    }
+    __syncwarp();
+    const int nsimp = min(P.N, nbest);
+    if (nbest <= 32) small_partial_sort(lst, nsimp, nbest, lane);
+    else if (lane == 0) partial_sort(lst, nsimp, nbest);
+    __syncwarp();
+    if (lane < P.N) {
+        unsigned oi = kNone;
+        if (lane < nsimp) {
+            int x, y, t;
+            unpack_xyt(lst[lane].i, rt, x, y, t);
+            oi = patch_index(P, x, y, t);
+        }
+        out_idx[(size_t)r * P.N + lane] = oi;
+        if (out_dist) out_dist[(size_t)r * P.N + lane] = lane < nsimp ? lst[lane].d : 0.f;
+    }
+    if (lane == 0) {
+        int thr = nsimp - 1;
+        while (lst[thr].d > P.tau && thr > 0) thr--;
+        unsigned pw2 = 1;
+        while (pw2 * 2 <= (unsigned)(thr + 1)) pw2 *= 2;
+        if (out_nsimp) out_nsimp[r] = (unsigned)nsimp;
+        out_nsx[r] = pw2;
+    }
+}
+
+}  // namespace
+
+// Shared-memory layout of the staged kernel; warp_bytes == 0 when the
+// shape is not handled by it.
+inline Layout bm2_layout(const StepHead& P)
+{
+    Layout L{0, 0, 0, 0};
+    if (!((P.k == 7 || P.k == 8) && (P.C == 1 || P.C == 3) && P.kt == 1 && P.bm_win_cap <= 64 && P.W <= 8192 &&
+          P.H <= 8192 && P.Nf <= 16))
+        return L;
+    const int p0 = bm2_pitch(P.Ns, P.k), p1 = bm2_pitch(P.Npr, P.k);
+    L.tile_floats = max(P.C * p0 * (P.Ns + P.k - 1), 2 * P.Nb * P.C * p1 * (P.Npr + P.k - 1));
+    L.tile_floats = (L.tile_floats + 3) & ~3;
+    L.res_cap = max(max(P.Ns * P.Ns, 2 * P.Nb * P.Npr * P.Npr), P.Nb * (1 + 2 * P.Nf));
+    L.scr_cap = max(P.Ns * P.Ns, P.Npr * P.Npr);
+    // the same sequence of 16-byte aligned regions as the kernel
+    size_t off = align16(sizeof(float2) * P.C * P.k * P.k);
+    off = align16(off + sizeof(float) * L.tile_floats);
+    off = align16(off + sizeof(Pair) * L.res_cap);
+    off = align16(off + sizeof(Pair) * L.scr_cap);
+    off = align16(off + sizeof(Pair) * 2 * P.Nb * P.Nb);
+    off = align16(off + sizeof(Pair) * P.bm_best_cap);
+    off = align16(off + sizeof(Win) * P.bm_win_cap);
+    off = align16(off + sizeof(PWin) * 2 * P.Nb);
+    off = align16(off + sizeof(unsigned) * 2 * kMaxNb);
+    off = align16(off + sizeof(int) * (3 + 2 * kMaxNb));
+    if (off > 24 * 1024) return L;
+    L.warp_bytes = (int)off;
+    return L;
+}
+
+}  // namespace vbm3d

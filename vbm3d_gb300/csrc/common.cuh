@@ -41,9 +41,9 @@ constexpr int kHADAMARD = 2;
 constexpr float kS2iHi = 0.70710676908493042f;          // float(0.7071067811865475)
 constexpr float kS2iLo = 1.2101617485882343e-08f;       // float(0.7071067811865475 - kS2iHi)
 
-// Everything a step kernel needs, passed by value (a few KB of kernel
-// parameter space).
-struct StepParams {
+// The scalar part of a step's parameters: everything block matching
+// needs, and all but the transform tables of the filter.
+struct StepHead {
     // video
     int W, H, F, C;
     unsigned wh, whc;
@@ -56,7 +56,12 @@ struct StepParams {
     long long ref_base;         // first reference of this launch (chunking)
     // noise per channel (estimate_sigma)
     float sigma[kMaxC];
-    // tables (k*k each, row-major)
+    // block-matching shared-memory layout (floats / pairs per warp)
+    int bm_list_cap, bm_best_cap, bm_win_cap, bm_warp_bytes;
+};
+
+// Transform tables of a step (k*k each, row-major, row stride k).
+struct StepTables {
     float kaiser[kMaxK * kMaxK];
     float fwd[kMaxK * kMaxK];   // DCT: 2cos(pi (j+1/2) u / k) [u][j]; bior: basis rows
     float inv[kMaxK * kMaxK];   // DCT: REDFT01 matrix [i][u]; bior: inverse basis rows
@@ -64,13 +69,15 @@ struct StepParams {
     float cni[kMaxK * kMaxK];
     float fwdT[kMaxK * kMaxK];  // transposes of fwd / inv (adjoint of the linearised filter)
     float invT[kMaxK * kMaxK];
-    // block-matching shared-memory layout (floats / pairs per warp)
-    int bm_list_cap, bm_best_cap, bm_win_cap, bm_warp_bytes;
 };
+
+// Everything a step kernel needs, passed by value (a few KB of kernel
+// parameter space).
+struct StepParams : StepHead, StepTables {};
 
 // Reference r of the grid, frames outer, then rows, then columns
 // (the loop order of src/vbm3d.cpp:527-538).
-__device__ __forceinline__ void ref_coords(const StepParams& P, long long r, int& x, int& y, int& t)
+__device__ __forceinline__ void ref_coords(const StepHead& P, long long r, int& x, int& y, int& t)
 {
     const long long per_frame = (long long)P.nrows * P.ncols;
     t = (int)(r / per_frame);
@@ -80,12 +87,12 @@ __device__ __forceinline__ void ref_coords(const StepParams& P, long long r, int
     x = min(jr * P.p, P.W - P.k);
 }
 
-__device__ __forceinline__ unsigned patch_index(const StepParams& P, int x, int y, int t)
+__device__ __forceinline__ unsigned patch_index(const StepHead& P, int x, int y, int t)
 {
     return (unsigned)t * P.whc + (unsigned)y * (unsigned)P.W + (unsigned)x;
 }
 
-__device__ __forceinline__ void patch_coords(const StepParams& P, unsigned idx, int& x, int& y, int& t)
+__device__ __forceinline__ void patch_coords(const StepHead& P, unsigned idx, int& x, int& y, int& t)
 {
     t = (int)(idx / P.whc);
     const unsigned r = idx - (unsigned)t * P.whc;   // channel 0: r < wh
@@ -97,7 +104,7 @@ __device__ __forceinline__ void patch_coords(const StepParams& P, unsigned idx, 
 // top-left corner of the patch's slice ht, for ht < kt.  Static unless mc;
 // with mc the corner follows the forward flow read at the previous corner,
 // accumulated in float and rounded (half away from zero) and clamped.
-__device__ __forceinline__ void trajectory(const StepParams& P, const float* __restrict__ fflow, int px, int py,
+__device__ __forceinline__ void trajectory(const StepHead& P, const float* __restrict__ fflow, int px, int py,
                                            int pt, int* tx, int* ty)
 {
     float fpx = (float)px, fpy = (float)py;
@@ -132,6 +139,22 @@ constexpr float kS2Lo = 2.4203234972131361e-08f;    // float(1.414213562373095 -
 __device__ __forceinline__ float mul_sqrt2(float s)
 {
     return __fmaf_rn(s, kS2Hi, __fmul_rn(s, kS2Lo));
+}
+
+// transformColorSpace of one RGB / YUV pixel (src/Utilities/LibVideoT.hpp:763-888),
+// float operations in the reference's order.
+__device__ __forceinline__ void color3(float& a, float& b, float& c, bool forward)
+{
+    const float R = a, G = b, B = c;
+    if (forward) {
+        a = 0.299f * R + 0.587f * G + 0.114f * B;
+        b = -0.14713f * R - 0.28886f * G + 0.436f * B;
+        c = 0.615f * R - 0.51498f * G - 0.10001f * B;
+    } else {
+        a = R + 1.13983f * B;
+        b = R - 0.39465f * G - 0.5806f * B;
+        c = R + 2.03211f * G;
+    }
 }
 
 struct Pair {

@@ -1,5 +1,6 @@
-// Device helpers shared by the filtering kernels (filter.cu) and the
-// linearised / adjoint kernels (linear.cu).
+// Device helpers shared by the filtering kernels (filter.cu), the batched
+// work kernels (batch_kernels.cuh) and the linearised / adjoint kernels
+// (linear.cu).
 #pragma once
 
 #include "common.cuh"
@@ -135,8 +136,8 @@ __device__ __forceinline__ void col_pass(float* x, const float* M)
 
 // Forward 2D transform of slice g (stride-1 K*K floats in shared memory),
 // through registers, result back in g.
-template <int K>
-__device__ __forceinline__ void slice_fwd2d(float* g, const StepParams& P)
+template <int K, class TT>
+__device__ __forceinline__ void slice_fwd2d(float* g, const StepHead& P, const TT& T)
 {
     float x[K * K];
 #pragma unroll
@@ -144,23 +145,23 @@ __device__ __forceinline__ void slice_fwd2d(float* g, const StepParams& P)
     if (K == 8 && P.T2D == kBIOR) {
         // bior_2d_forward (src/lib_transforms.cpp:158-176): t = X B^T (rows),
         // out[i][j] = sum_q t[q][i] B[j][q], i.e. the column pass gives out^T
-        row_pass<K, true>(x, P.fwd);
-        col_pass<K, true>(x, P.fwd);
+        row_pass<K, true>(x, T.fwd);
+        col_pass<K, true>(x, T.fwd);
 #pragma unroll
         for (int i = 0; i < K; i++)
 #pragma unroll
             for (int j = 0; j < K; j++) g[i * K + j] = x[j * K + i];
     } else {
         // REDFT10 along rows then columns, then coef_norm (src/vbm3d.cpp:1294-1302)
-        row_pass<K, false>(x, P.fwd);
-        col_pass<K, false>(x, P.fwd);
+        row_pass<K, false>(x, T.fwd);
+        col_pass<K, false>(x, T.fwd);
 #pragma unroll
-        for (int e = 0; e < K * K; e++) g[e] = x[e] * P.cn[e];
+        for (int e = 0; e < K * K; e++) g[e] = x[e] * T.cn[e];
     }
 }
 
-template <int K>
-__device__ __forceinline__ void slice_inv2d(float* g, const StepParams& P)
+template <int K, class TT>
+__device__ __forceinline__ void slice_inv2d(float* g, const StepHead& P, const TT& T)
 {
     float x[K * K];
 #pragma unroll
@@ -169,8 +170,8 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepParams& P)
         // bior_2d_inverse (src/lib_transforms.cpp:294-320): temp = in^T;
         // t2 = temp B^T, computed as a column pass on `in` (gives t2^T);
         // then the row pass gives temp[i][j]; signal[j][i] = temp[i][j]
-        col_pass<K, true>(x, P.inv);
-        row_pass<K, true>(x, P.inv);
+        col_pass<K, true>(x, T.inv);
+        row_pass<K, true>(x, T.inv);
 #pragma unroll
         for (int i = 0; i < K; i++)
 #pragma unroll
@@ -178,9 +179,9 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepParams& P)
     } else {
         // dct_2d_inv (src/vbm3d.cpp:1696-1709)
 #pragma unroll
-        for (int e = 0; e < K * K; e++) x[e] = x[e] * P.cni[e];
-        row_pass<K, false>(x, P.inv);
-        col_pass<K, false>(x, P.inv);
+        for (int e = 0; e < K * K; e++) x[e] = x[e] * T.cni[e];
+        row_pass<K, false>(x, T.inv);
+        col_pass<K, false>(x, T.inv);
         const float coef = 1.0f / (float)(K * 2);
 #pragma unroll
         for (int e = 0; e < K * K; e++) g[e] = coef * x[e];
@@ -192,7 +193,7 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepParams& P)
 // memory, so a warp load touches a few rows instead of 32 patches).  idx[n]
 // is the patch's linear index in channel 0; log2n = log2(nsx).
 template <int K, int SS>
-__device__ __forceinline__ void gather_k(const StepParams& P, const float* __restrict__ vid, const unsigned* idx,
+__device__ __forceinline__ void gather_k(const StepHead& P, const float* __restrict__ vid, const unsigned* idx,
                                          int nsx, int log2n, float* g, int lane)
 {
     constexpr int K2 = K * K;
@@ -202,6 +203,194 @@ __device__ __forceinline__ void gather_k(const StepParams& P, const float* __res
         const int c = sl >> log2n, n = sl & (nsx - 1);
         const int p = pq / K, q = pq - p * K;
         g[sl * SS + pq] = __ldg(vid + idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q);
+    }
+}
+
+// ---------------------------------------------------------------- 1D ---
+
+// Step 1 shrinkage of one coefficient vector (all n at one (c, pq)):
+// ht_filtering_haar / _hadamard (src/vbm3d.cpp:1405-1521).  Returns the
+// number of kept coefficients.
+template <int N>
+__device__ __forceinline__ int ht_vector(float* g, int stride, bool is_dc_pos, float T, int T3D)
+{
+    float v[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) v[n] = g[n * stride];
+    int kept = 0;
+    if (T3D == kHADAMARD) {
+        hadamard<N>(v);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            if ((is_dc_pos && n == 0) || fabsf(v[n]) > T) kept++;
+            else v[n] = 0.0f;
+        }
+        hadamard<N>(v);
+        const float coef = 1.0f / (float)N;
+#pragma unroll
+        for (int n = 0; n < N; n++) v[n] = v[n] * coef;
+    } else {
+        haar_fwd<N>(v);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            if ((is_dc_pos && n == 0) || fabsf(v[n]) > T) kept++;
+            else v[n] = 0.0f;
+        }
+        haar_inv<N>(v);
+    }
+#pragma unroll
+    for (int n = 0; n < N; n++) g[n * stride] = v[n];
+    return kept;
+}
+
+// Step 2 shrinkage: wiener_filtering_haar / _hadamard
+// (src/vbm3d.cpp:1539-1666, DCWIENER on).  Writes the estimate into gb and
+// returns the sum of squared Wiener coefficients.
+template <int N>
+__device__ __forceinline__ float wiener_vector(const float* gn, float* gb, int stride, float s2, int T3D)
+{
+    float vn[N], vb[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+        vn[n] = gn[n * stride];
+        vb[n] = gb[n * stride];
+    }
+    float wsum = 0.f;
+    if (T3D == kHADAMARD) {
+        hadamard<N>(vn);
+        hadamard<N>(vb);
+        const float coef = 1.0f / (float)N;
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            float value = vb[n] * vb[n] * coef;
+            value = value / (value + s2);
+            vb[n] = vn[n] * value * coef;
+            wsum = wsum + value * value;
+        }
+        hadamard<N>(vb);
+    } else {
+        haar_fwd<N>(vn);
+        haar_fwd<N>(vb);
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            float value = vb[n] * vb[n];
+            value = value / (value + s2);
+            vb[n] = vn[n] * value;
+            wsum = wsum + value * value;
+        }
+        haar_inv<N>(vb);
+    }
+#pragma unroll
+    for (int n = 0; n < N; n++) gb[n * stride] = vb[n];
+    return wsum;
+}
+
+// 1D transform along the group, shrinkage and the per-channel weights of
+// one group held in shared memory as slices [c][n][k*k] of stride ss; one
+// coefficient vector (c, pq) per lane.
+template <int STEP, int NMAX = 32>
+__device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB, int nsx, int ss, int lane,
+                                        float* wgt)
+{
+    // slices are laid out [c][n][ht][k*k] with stride ss; the coefficient
+    // vector (c, ht, pq) runs over n with stride kt*ss.  Its index in the
+    // reference's group_3D is pq + ht*k*k, so the group DC is pq = ht = 0.
+    const int k2 = P.k * P.k, kt = P.kt, k2t = k2 * kt, C = P.C, ns = kt * ss;
+    float acc[kMaxC] = {0.f, 0.f, 0.f};
+    for (int v = lane; v < C * k2t; v += 32) {
+        const int c = v / k2t, rem = v - c * k2t, ht = rem / k2, pq = rem - ht * k2;
+        float* ga = gA + ((size_t)(c * nsx) * kt + ht) * ss + pq;
+        float* gb = gB + ((size_t)(c * nsx) * kt + ht) * ss + pq;
+        const bool dc = pq == 0 && ht == 0;
+        if (STEP == 1) {
+            const float T = P.lambda3D * P.sigma[c] * (P.T3D == kHADAMARD ? sqrtf((float)nsx) : 1.0f);
+            int kept;
+            switch (nsx) {
+                case 1: kept = ht_vector<1>(ga, ns, dc, T, P.T3D); break;
+                case 2: kept = ht_vector<2>(ga, ns, dc, T, P.T3D); break;
+                case 4: kept = ht_vector<4>(ga, ns, dc, T, P.T3D); break;
+                case 8: kept = ht_vector<(NMAX < 8 ? NMAX : 8)>(ga, ns, dc, T, P.T3D); break;
+                case 16: kept = ht_vector<(NMAX < 16 ? NMAX : 16)>(ga, ns, dc, T, P.T3D); break;
+                default: kept = ht_vector<NMAX>(ga, ns, dc, T, P.T3D); break;
+            }
+            acc[c] += (float)kept;
+        } else {
+            const float s2 = P.sigma[c] * P.sigma[c];
+            float ws;
+            switch (nsx) {
+                case 1: ws = wiener_vector<1>(ga, gb, ns, s2, P.T3D); break;
+                case 2: ws = wiener_vector<2>(ga, gb, ns, s2, P.T3D); break;
+                case 4: ws = wiener_vector<4>(ga, gb, ns, s2, P.T3D); break;
+                case 8: ws = wiener_vector<(NMAX < 8 ? NMAX : 8)>(ga, gb, ns, s2, P.T3D); break;
+                case 16: ws = wiener_vector<(NMAX < 16 ? NMAX : 16)>(ga, gb, ns, s2, P.T3D); break;
+                default: ws = wiener_vector<NMAX>(ga, gb, ns, s2, P.T3D); break;
+            }
+            acc[c] += ws;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxC; c++) {
+        const float tot = warp_sum(acc[c]);  // counts are exact; Wiener sums reassociate
+        const float s2 = P.sigma[c] * P.sigma[c];
+        if (STEP == 2 && P.T3D == kHADAMARD) wgt[c] = tot > 0.0f ? 1.0f / (float)(s2 * tot) : 1.0f;
+        else wgt[c] = 1.f / (float)(s2 * tot);
+    }
+    __syncwarp();
+
+}
+
+template <int K, int SS, class TT>
+__device__ __forceinline__ void slice_fwd(const StepHead& P, const TT& T, float* g, int nsl, int lane)
+{
+    for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(g + sl * SS, P, T);
+}
+
+// Filtering and aggregation of the group of reference patch r by one warp,
+// register-resident transforms for compile-time K (kt == 1, N <= 8), with
+// the warp's shared-memory region `base`.  T holds the kaiser / fwd / inv /
+// cn / cni tables (StepParams, or the batched form's compact copy).
+template <int STEP, int K, bool PAIR, class TT>
+__device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long long r, float* base, int lane,
+                                           const float* __restrict__ noisy, const float* __restrict__ basic,
+                                           const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
+                                           const AggTarget& A)
+{
+    constexpr int K2 = K * K, SS = K2 + 1;
+    const int C = P.C;
+    unsigned* idx = reinterpret_cast<unsigned*>(base);
+    float* gA = base + kMaxN;               // noisy group
+    float* gB = gA + (size_t)C * P.N * SS;  // basic group (step 2)
+
+    const int nsx = (int)tab_nsx[r];
+    const int log2n = __ffs(nsx) - 1;
+    if (lane < nsx) idx[lane] = tab_idx[(size_t)r * P.N + lane];
+    __syncwarp();
+    const int nsl = C * nsx;
+
+    gather_k<K, SS>(P, noisy, idx, nsx, log2n, gA, lane);
+    if (STEP == 2) gather_k<K, SS>(P, basic, idx, nsx, log2n, gB, lane);
+    __syncwarp();
+    // 2D transforms, one slice (c, n) per lane, in registers
+    slice_fwd<K, SS>(P, T, gA, nsl, lane);
+    if (STEP == 2) slice_fwd<K, SS>(P, T, gB, nsl, lane);
+    __syncwarp();
+
+    float wgt[kMaxC];
+    group_1d<STEP, 8>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
+
+    // inverse 2D, one slice per lane
+    float* ge = STEP == 1 ? gA : gB;
+    for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(ge + sl * SS, P, T);
+    __syncwarp();
+
+    // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
+    const int total = nsl * K2;
+    for (int e = lane; e < total; e += 32) {
+        const int sl = e / K2, pq = e - sl * K2;
+        const int c = sl >> log2n, n = sl & (nsx - 1);
+        const int p = pq / K, q = pq - p * K;
+        const float kw = T.kaiser[pq] * wgt[c];
+        agg_add<PAIR>(A, idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q, kw * ge[sl * SS + pq], kw);
     }
 }
 

@@ -222,7 +222,7 @@ linear_kernel(const StepParams P, const float* __restrict__ src, const float* __
 
     gather_k<K, SS>(P, src, idx, nsx, log2n, gS, lane);
     __syncwarp();
-    for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gS + sl * SS, P);
+    for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gS + sl * SS, P, P);
     __syncwarp();
     float wgt[kMaxC];
     gains_group<STEP, 8>(P, gS, nsx, SS, lane, wgt);
@@ -230,10 +230,10 @@ linear_kernel(const StepParams P, const float* __restrict__ src, const float* __
     if (!ADJ) {
         gather_k<K, SS>(P, x, idx, nsx, log2n, gX, lane);
         __syncwarp();
-        for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gX + sl * SS, P);
+        for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gX + sl * SS, P, P);
         __syncwarp();
         apply_group<STEP, 8>(P, gX, gS, nsx, SS, lane);
-        for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(gX + sl * SS, P);
+        for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(gX + sl * SS, P, P);
         __syncwarp();
         const AggTarget A{nullptr, nullptr, out};
         for (int e = lane; e < nsl * K2; e += 32) {

@@ -53,8 +53,7 @@ __global__ void normalize_pair_kernel(const float2* __restrict__ pair, const flo
     }
 }
 
-// transformColorSpace, 3 channels (src/Utilities/LibVideoT.hpp:763-888);
-// float operations in the reference's order.
+// transformColorSpace, 3 channels, in place (color3 in common.cuh).
 __global__ void color_kernel(float* __restrict__ v, unsigned wh, unsigned frames, int forward)
 {
     const size_t n = (size_t)wh * frames;
@@ -63,17 +62,8 @@ __global__ void color_kernel(float* __restrict__ v, unsigned wh, unsigned frames
         float* r = v + f * 3 * (size_t)wh + k;
         float* g = r + wh;
         float* b = g + wh;
-        const float R = *r, G = *g, B = *b;
-        float o0, o1, o2;
-        if (forward) {
-            o0 = 0.299f * R + 0.587f * G + 0.114f * B;
-            o1 = -0.14713f * R - 0.28886f * G + 0.436f * B;
-            o2 = 0.615f * R - 0.51498f * G - 0.10001f * B;
-        } else {
-            o0 = R + 1.13983f * B;
-            o1 = R - 0.39465f * G - 0.5806f * B;
-            o2 = R + 2.03211f * G;
-        }
+        float o0 = *r, o1 = *g, o2 = *b;
+        color3(o0, o1, o2, forward != 0);
         *r = o0;
         *g = o1;
         *b = o2;
