@@ -1,17 +1,25 @@
 """VBM3D throughput benchmark (both steps, run_vbm3d semantics).
 
-Workload: 1920x1080 x 30 frames RGB, AWGN sigma = 30, reference default
-parameters for both steps, colour transform on (the reference CLI's
-default), no flow; seeded synthetic clip (vbm3d_gb300.synth, seed 3000,
-motion <= 6 px/frame) in place of a dataset.
+Default workload (--workload batch64): the batched form on 64 clips of
+uneven size, width uniform in 160-1280, height in 120-720, 5-40 frames, 1
+or 3 channels, sigma in {5, 10, 20, 30, 50}; shapes drawn from numpy
+PCG64(4000), each clip from the seeded synthetic generator
+(vbm3d_gb300.synth, seed 4000 + clip) in place of a dataset; reference
+default parameters for both steps, colour transform on, no flow.
+--workload 1080p30: the plain path on one RGB 1920x1080 x 30 clip, sigma 30
+(seed 3000, motion <= 6 px/frame).
 
-Metric: denoised Mpix-frames/s = W*H*F / 1e6 / time of (step 1 + step 2).
-  value : device-resident (inputs already in HBM; every step restores the
-          noisy input on the device, runs both passes, and leaves basic and
-          final estimates in HBM).  The clip (746 MB) is larger than L2.
-  e2e   : the same work through vbm3d_run_host (the C-ABI call a CPU caller
-          makes) from pinned host memory: H2D of the noisy clip and D2H of
-          the basic and final estimates inside every timed step.
+Metric: denoised Mpix-frames/s = sum of W*H*F / 1e6 / time of (step 1 +
+step 2) over every clip.
+  value : device-resident (inputs already in HBM, 2.7 GB for batch64 and
+          0.75 GB for 1080p30, both larger than L2): one CUDA-graph launch
+          of the whole batch per step (batch64), one vbm3d_gpu_run per step
+          (1080p30).
+  plain : (batch64) the same clips looped through vbm3d_gpu_run, and the
+          largest PSNR difference between the two forms.
+  e2e   : the same work from pinned host memory through the public API:
+          H2D of every noisy clip, the run, D2H of the basic and final
+          estimates, all inside every timed step.
 Multi-GPU: the path has no exchange step; --gpus N runs N independent
 replicas (one per rank) and value = total clip frames / max time.
 
@@ -30,15 +38,23 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "denoised Mpix-frames/s (both steps), batched vs plain at <=0.01 dB PSNR delta"
+UNIT = "Mpix-frames/s"
+COLOR = True
+DATA = "synthetic (seeded blobs/gratings/translation + AWGN)"
+
+# 1080p30 plain workload
 W, H, F, C = 1920, 1080, 30, 3
 SIGMA = 30.0
 SEED = 3000
-COLOR = True
-# CPU sample: a centre crop of the same clip with all 30 frames
+WORKLOAD_1080 = "plain VBM3D, RGB 1920x1080x30, sigma=30, reference default parameters, colour transform on, no flow"
+WORKLOAD_BATCH = ("batched VBM3D, 64 clips: width U[160,1280], height U[120,720], 5-40 frames, 1 or 3 channels, "
+                  "sigma in {5,10,20,30,50}; reference default parameters, colour transform on, no flow")
+
+# CPU sample: centre crops of this size (at most) of every 8th clip
+SAMPLE_W, SAMPLE_H, SAMPLE_F = 256, 144, 8
+# 1080p30 CPU sample: a centre crop with all 30 frames
 CROP_W, CROP_H = 480, 270
-METRIC = "denoised Mpix-frames/s (both steps)"
-UNIT = "Mpix-frames/s"
-WORKLOAD = "plain VBM3D, RGB 1920x1080x30, sigma=30, reference default parameters, colour transform on, no flow"
 
 
 def parse():
@@ -47,21 +63,49 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "1080p30"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-1080p", action="store_true", help="batch64: skip the extra 1080p30 plain figure")
     return ap.parse_args()
 
 
-def make_workload():
+def batch_specs():
+    """(width, height, frames, channels, sigma) of the 64 clips."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(4000))
+    out = []
+    for _ in range(64):
+        w = int(rng.integers(160, 1281))
+        h = int(rng.integers(120, 721))
+        f = int(rng.integers(5, 41))
+        c = int(rng.choice([1, 3]))
+        s = float(rng.choice([5, 10, 20, 30, 50]))
+        out.append((w, h, f, c, s))
+    return out
+
+
+def make_batch():
+    from vbm3d_gb300.synth import make_clip
+    clips = []
+    for i, (w, h, f, c, s) in enumerate(batch_specs()):
+        clean, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)
+        clips.append(dict(clean=clean, noisy=noisy, sigma=s))
+    return clips
+
+
+def make_1080():
     from vbm3d_gb300.synth import make_clip
     clean, noisy, _, _ = make_clip(W, H, F, C, SIGMA, SEED, vmax=6.0)
     return clean, noisy
 
 
-def crop(noisy):
+def crop(v, w, h, f):
     import numpy as np
-    y0, x0 = (H - CROP_H) // 2, (W - CROP_W) // 2
-    return np.ascontiguousarray(noisy[:, :, y0:y0 + CROP_H, x0:x0 + CROP_W])
+    F_, _, H_, W_ = v.shape
+    w, h, f = min(w, W_), min(h, H_), min(f, F_)
+    y0, x0 = (H_ - h) // 2, (W_ - w) // 2
+    return np.ascontiguousarray(v[:f, :, y0:y0 + h, x0:x0 + w])
 
 
 def cpu_threads():
@@ -71,18 +115,33 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def time_cpu_sample(noisy_crop, steps=1):
-    """Oracle port on the crop with all host threads; returns (Mpix-frames/s, threads)."""
+def time_cpu(samples, steps=1):
+    """Oracle port over [(noisy, sigma)] with all host threads; returns
+    (Mpix-frames/s, threads)."""
     from oracle.pyoracle import Oracle
     o = Oracle()
     th = cpu_threads()
-    p1, p2 = o.default_params(1, SIGMA), o.default_params(2, SIGMA)
+    mpf = 0.0
     t0 = time.perf_counter()
     for _ in range(steps):
-        o.run(SIGMA, noisy_crop, p1, p2, color_space=COLOR, threads=th)
-    dt = time.perf_counter() - t0
-    f, _, h, w = noisy_crop.shape
-    return w * h * f * steps / 1e6 / dt, th
+        for noisy, sigma in samples:
+            o.run(sigma, noisy, o.default_params(1, sigma), o.default_params(2, sigma), color_space=COLOR,
+                  threads=th)
+            f, _, h, w = noisy.shape
+            mpf += w * h * f / 1e6
+    return mpf / (time.perf_counter() - t0), th
+
+
+def cpu_sample(workload, clips=None, noisy=None):
+    """The bounded CPU sample of a workload and its description."""
+    if workload == "batch64":
+        picks = list(range(0, 64, 8))
+        samples = [(crop(clips[i]["noisy"], SAMPLE_W, SAMPLE_H, SAMPLE_F), clips[i]["sigma"]) for i in picks]
+        mpf = sum(a.shape[0] * a.shape[2] * a.shape[3] for a, _ in samples) / 1e6
+        return samples, ("centre crops (at most %dx%dx%d) of clips %s, %.2f Mpix-frames, both steps"
+                         % (SAMPLE_W, SAMPLE_H, SAMPLE_F, picks, mpf))
+    c = crop(noisy, CROP_W, CROP_H, F)
+    return [(c, SIGMA)], "%dx%dx%d centre crop of the workload, both steps" % (CROP_W, CROP_H, F)
 
 
 class ClockSampler:
@@ -167,27 +226,80 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    _, noisy = make_workload()
-    sample = crop(noisy)
-    time_cpu_sample(sample[:4], steps=1) if args.warmup > 0 else None
-    value, th = time_cpu_sample(sample, steps=args.steps)
-    f, _, h, w = sample.shape
+    if args.workload == "batch64":
+        samples, desc = cpu_sample("batch64", clips=make_batch())
+        workload = WORKLOAD_BATCH
+    else:
+        _, noisy = make_1080()
+        samples, desc = cpu_sample("1080p30", noisy=noisy)
+        workload = WORKLOAD_1080
+    if args.warmup > 0:
+        time_cpu([(a[:2], s) for a, s in samples[:2]])
+    value, th = time_cpu(samples, steps=args.steps)
+    mpf = sum(a.shape[0] * a.shape[2] * a.shape[3] for a, _ in samples) / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "ms_per_step": round(w * h * f / 1e6 / value * 1e3, 1), "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded blobs/gratings/translation + AWGN)",
-        "config": {"workload": WORKLOAD, "sample": "%dx%dx%d centre crop" % (w, h, f)},
+        "ms_per_step": round(mpf / value * 1e3, 1), "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": {"workload": workload, "sample": desc},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": th, "kind": "port",
-                         "sample": "%dx%dx%d centre crop of the workload, both steps, %d OpenMP threads"
-                                   % (w, h, f, th)},
+                         "sample": desc + ", %d OpenMP threads" % th},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def bm_flops(p, dims_video, n_dist):
-    return float(n_dist) * p.k * p.k * p.kt * dims_video.channels * 3.0  # sub, mul, add per term
+def bm_flops(k, channels, n_dist):
+    return float(n_dist) * k * k * channels * 3.0  # sub, mul, add per term (kt = 1)
+
+
+def fp32_peak(dev, clocks):
+    import torch
+    sm_max = clocks.get("sm_max_mhz") or 2070.0
+    try:
+        sm_max = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("sm_max_mhz", sm_max)
+    except (OSError, ValueError):
+        pass
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    return n_sm * 128 * 2 * sm_max * 1e6 / 1e12, "nominal FP32 FMA rate: %d SMs x 128 lanes x 2 x %.0f MHz" % (
+        n_sm, sm_max)
+
+
+# DRAM bytes (read + write) per reference patch of the batched step-2 block
+# matching of RGB k = 7 clips, from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3> / its references) on
+# the profile case of vbm3d_gb300.profile_case --batch.
+BM2_DRAM_BYTES_PER_REF = None
+
+
+def timed(stream, fn, steps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measure_1080(vb, dev, steps, warmup, full):
+    """The plain 1080p30 workload; with full, also the roofline inputs."""
+    import torch
+    clean, noisy = make_1080()
+    p1, p2 = vb.default_params(1, SIGMA), vb.default_params(2, SIGMA)
+    x0 = torch.from_numpy(noisy).to(dev)
+    x = torch.empty_like(x0)
+    out = {}
+
+    def one_step():
+        x.copy_(x0)
+        out["bf"] = vb.run(x, SIGMA, p1, p2, color_space=COLOR)
+
+    for _ in range(max(warmup, 0)):
+        one_step()
+    torch.cuda.synchronize()
+    return clean, noisy, x0, one_step, out, p1, p2
 
 
 def run_gpu(args):
@@ -195,118 +307,211 @@ def run_gpu(args):
     import torch
 
     import vbm3d_gb300 as vb
+    from vbm3d_gb300.synth import psnr
 
     rank, world = dist_setup(args.gpus)
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    vb.load()
-
-    clean, noisy = make_workload()
-    p1, p2 = vb.default_params(1, SIGMA), vb.default_params(2, SIGMA)
-    x0 = torch.from_numpy(noisy).to(dev)
-    x = torch.empty_like(x0)
     stream = torch.cuda.current_stream()
+    vb.load()
+    line = {}
 
-    def one_step():
-        x.copy_(x0)
-        return vb.run(x, SIGMA, p1, p2, color_space=COLOR)
-
-    for _ in range(max(args.warmup, 0)):
-        basic, final = one_step()
-    torch.cuda.synchronize()
-
-    # timed region: K steps, barrier + synchronize on both sides
-    sampler = ClockSampler(local)
-    barrier(world)
-    torch.cuda.synchronize()
-    sampler.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        basic, final = one_step()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    barrier(world)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    ms = reduce_max(ms, world)
-    mpf = W * H * F / 1e6
-    value = mpf * world / (ms / 1e3)
-    launches_per_step = 2 + 2 + 2 + (4 if COLOR else 0)  # bm, filter, normalize per step; colour transforms
-
-    # quality of this run (not part of the timed region)
-    from vbm3d_gb300.synth import psnr
-    final_np = final.cpu().numpy()
-    q = {"psnr_noisy": round(psnr(clean, noisy), 3), "psnr_final": round(psnr(clean, final_np), 3)}
-
-    # roofline of the dominant kernel: step-2 block matching on the basic
-    # estimate (in the colour space the step sees), timed alone on the stream
-    xb = torch.from_numpy(noisy).to(dev)
-    vb.color_transform(xb, True)
-    b_ws = basic.clone()
-    vb.color_transform(b_ws, True)
-    n_dist = vb.bm_distance_count(b_ws, p2)
-    d_video = vb.Dims(W, H, F, C)
-    flops = bm_flops(p2, d_video, n_dist)
-    reps = 3
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    vb.similar_patches(b_ws, p2)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(reps):
-        vb.similar_patches(b_ws, p2)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    bm_ms = e0.elapsed_time(e1) / reps
-    sm_max = clocks.get("sm_max_mhz") or 2070.0
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        sm_max = peaks.get("sm_max_mhz", sm_max)
-    except (OSError, ValueError):
-        pass
-    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FMA = 2 flops
-    achieved = flops / (bm_ms / 1e3) / 1e12
-    roofline = {"kernel": "bm_kernel (step-2 block matching)", "bound": "fp32", "achieved": round(achieved, 3),
-                "peak": round(fp32_peak, 1), "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4),
-                "traffic": None, "peak_source": "nominal FP32 FMA rate: %d SMs x 128 lanes x 2 x %.0f MHz" % (n_sm, sm_max),
-                "algorithmic_flops": flops, "distances": n_dist, "ms": round(bm_ms, 3)}
-
-    # end to end through the host C-ABI call, pinned host buffers
-    e2e = None
-    if args.e2e_steps > 0:
-        hn = torch.from_numpy(noisy).pin_memory().numpy()
-        hb = torch.empty(noisy.shape, dtype=torch.float32).pin_memory().numpy()
-        hf = torch.empty(noisy.shape, dtype=torch.float32).pin_memory().numpy()
-        vb.run_host(hn, SIGMA, p1, p2, color_space=COLOR, basic=hb, out=hf)
-        barrier(world)
+    if args.workload == "batch64":
+        clips = make_batch()
+        mpf = sum(c["noisy"].shape[0] * c["noisy"].shape[2] * c["noisy"].shape[3] for c in clips) / 1e6
+        x0 = [torch.from_numpy(c["noisy"]).to(dev) for c in clips]
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            vb.run_host(hn, SIGMA, p1, p2, color_space=COLOR, basic=hb, out=hf)
-        dt = (time.perf_counter() - t0) / args.e2e_steps
-        dt = reduce_max(dt, world)
-        e2e = {"value": round(mpf * world / dt, 3), "unit": UNIT, "h2d_bytes_per_step": int(hn.nbytes),
-               "d2h_bytes_per_step": int(hb.nbytes + hf.nbytes), "ms_per_step": round(dt * 1e3, 1)}
+        b = vb.Batch([dict(noisy=x, sigma=c["sigma"]) for x, c in zip(x0, clips)], color_space=COLOR)
+        torch.cuda.synchronize()
+        create_s = time.perf_counter() - t0
+        cfg = b.config()
+        for _ in range(max(args.warmup, 0)):
+            b.run()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local)
+        barrier(world)
+        torch.cuda.synchronize()
+        sampler.start()
+        ms = timed(stream, b.run, args.steps)
+        clocks = sampler.stop()
+        barrier(world)
+        ms = reduce_max(ms, world)
+        value = mpf * world / (ms / 1e3)
+        launches = b.profile()
+        gpu_launches = (len(launches) + 3) * args.steps  # work launches + prep, mid, final
+        batched_final = [d.cpu().numpy() for d in b.denoised]
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        sample = crop(noisy)
-        val, th = time_cpu_sample(sample, steps=1)
-        f, _, h, w = sample.shape
-        cpu = {"value": round(val, 4), "unit": UNIT, "cores": th, "kind": "port",
-               "sample": "%dx%dx%d centre crop of the workload, both steps, %d OpenMP threads" % (w, h, f, th)}
+        # the plain path looped over the same clips (vbm3d_gpu_run transforms
+        # its input in place and back, so every step restores it first)
+        xs = [torch.empty_like(x) for x in x0]
+        outs = []
 
-    if rank == 0:
+        def plain_step():
+            outs.clear()
+            for x, xi, c in zip(xs, x0, clips):
+                x.copy_(xi)
+                outs.append(vb.run(x, c["sigma"], color_space=COLOR))
+
+        plain_step()
+        torch.cuda.synchronize()
+        plain_ms = timed(stream, plain_step, 2)
+        dps, gain = 0.0, []
+        for c, bf, (_, pf) in zip(clips, batched_final, outs):
+            pb = psnr(c["clean"], bf)
+            dps = max(dps, abs(pb - psnr(c["clean"], pf.cpu().numpy())))
+            gain.append(pb - psnr(c["clean"], c["noisy"]))
+        plain = {"value": round(mpf * world / (plain_ms / 1e3), 3), "unit": UNIT, "ms_per_step": round(plain_ms, 1),
+                 "psnr_delta_max_db": round(dps, 5), "what": "the same clips looped through vbm3d_gpu_run"}
+
+        # roofline: the dominant block-matching launch of the batch
+        bm = max((l for l in launches if l["phase"] in (0, 2)), key=lambda l: l["ms"])
+        top = max(launches, key=lambda l: l["ms"])
+        step = bm["phase"] // 2 + 1
+        members = [i for i, c in enumerate(clips)
+                   if vb.default_params(step, c["sigma"]).k == bm["k"] and c["noisy"].shape[1] == bm["channels"]]
+        n_dist = 0
+        for i in members:
+            c = clips[i]
+            p1, p2 = vb.default_params(1, c["sigma"]), vb.default_params(2, c["sigma"])
+            x = x0[i].clone()
+            vb.color_transform(x, COLOR)
+            if step == 1:
+                n_dist += vb.bm_distance_count(x, p1)
+            else:
+                num, den = vb.step1(x, p1, c["sigma"], color_space=COLOR)
+                n_dist += vb.bm_distance_count(vb.normalize(num, den, x), p2)
+        flops = bm_flops(bm["k"], bm["channels"], n_dist)
+        peak, peak_src = fp32_peak(dev, clocks)
+        achieved = flops / (bm["ms"] / 1e3) / 1e12
+        traffic = None if BM2_DRAM_BYTES_PER_REF is None or (step, bm["k"], bm["channels"]) != (2, 7, 3) \
+            else BM2_DRAM_BYTES_PER_REF * bm["refs"]
+        roofline = {"kernel": "batch_bm_kernel<%d, %d, %d> (step-%d block matching, %d clips)"
+                              % (step, bm["k"], bm["channels"], step, bm["clips"]),
+                    "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
+                    "algorithmic_flops": flops, "distances": n_dist, "refs": bm["refs"], "ms": round(bm["ms"], 2),
+                    "share_of_run": round(bm["ms"] / sum(l["ms"] for l in launches), 3),
+                    "largest_launch": "phase %d k=%d C=%d, %.1f ms" % (top["phase"], top["k"], top["channels"],
+                                                                      top["ms"])}
+
+        # end to end through the public API from pinned host memory
+        e2e = None
+        if args.e2e_steps > 0:
+            hin = [torch.from_numpy(c["noisy"]).pin_memory() for c in clips]
+            hb = [torch.empty(c["noisy"].shape, dtype=torch.float32).pin_memory() for c in clips]
+            hd = [torch.empty(c["noisy"].shape, dtype=torch.float32).pin_memory() for c in clips]
+
+            def e2e_step():
+                for x, h in zip(x0, hin):
+                    x.copy_(h, non_blocking=True)
+                b.run()
+                for ob, od, db, dd in zip(hb, hd, b.basic, b.denoised):
+                    ob.copy_(db, non_blocking=True)
+                    od.copy_(dd, non_blocking=True)
+                torch.cuda.synchronize()
+
+            e2e_step()
+            barrier(world)
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                e2e_step()
+            dt = reduce_max((time.perf_counter() - t0) / args.e2e_steps, world)
+            nb = sum(h.numel() * 4 for h in hin)
+            e2e = {"value": round(mpf * world / dt, 3), "unit": UNIT, "h2d_bytes_per_step": nb,
+                   "d2h_bytes_per_step": 2 * nb, "ms_per_step": round(dt * 1e3, 1),
+                   "what": "pinned host -> device copies of the 64 noisy clips, one batch run, device -> pinned "
+                           "host copies of the basic and final estimates"}
+
+        extra_1080 = None
+        if not args.no_1080p:
+            clean, noisy, _, one_step, out, _, _ = measure_1080(vb, dev, 2, 2, False)
+            ms1080 = timed(stream, one_step, 3)
+            extra_1080 = {"workload": WORKLOAD_1080, "value": round(W * H * F / 1e6 / (ms1080 / 1e3), 3),
+                          "unit": UNIT, "ms_per_step": round(ms1080, 1),
+                          "psnr_final": round(psnr(clean, out["bf"][1].cpu().numpy()), 3)}
+
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            samples, desc = cpu_sample("batch64", clips=clips)
+            val, th = time_cpu(samples)
+            cpu = {"value": round(val, 4), "unit": UNIT, "cores": th, "kind": "port",
+                   "sample": desc + ", %d OpenMP threads" % th}
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded blobs/gratings/translation + AWGN)",
-            "config": {"workload": WORKLOAD, "global_batch": world, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (746 MB clip)", "quality": q},
-            "clocks": clocks, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
-            "roofline": roofline, "cpu_baseline": cpu,
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {"workload": WORKLOAD_BATCH, "clips": len(clips), "mpix_frames": round(mpf, 2),
+                       "global_batch": world, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (%.1f GB)" % (sum(x.numel() for x in x0) * 4 / 1e9),
+                       "graph": "one CUDA-graph launch per step", "tuned": {k: cfg[k] for k in cfg
+                                                                            if k.endswith(("tile", "warps"))},
+                       "create_s": round(create_s, 2),
+                       "psnr_gain_db": {"min": round(min(gain), 3), "mean": round(float(np.mean(gain)), 3)}},
+            "plain": plain, "clocks": clocks, "e2e": e2e, "gpu_launches": gpu_launches, "roofline": roofline,
+            "cpu_baseline": cpu, "plain_1080p30": extra_1080,
+            "launches": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in l.items()
+                          if k in ("phase", "k", "channels", "clips", "refs", "ms")} for l in launches],
         }
+    else:
+        clean, noisy, x0, one_step, out, p1, p2 = measure_1080(vb, dev, args.steps, args.warmup, True)
+        sampler = ClockSampler(local)
+        barrier(world)
+        torch.cuda.synchronize()
+        sampler.start()
+        ms = timed(stream, one_step, args.steps)
+        clocks = sampler.stop()
+        barrier(world)
+        ms = reduce_max(ms, world)
+        mpf = W * H * F / 1e6
+        value = mpf * world / (ms / 1e3)
+        basic, final = out["bf"]
+        q = {"psnr_noisy": round(psnr(clean, noisy), 3), "psnr_final": round(psnr(clean, final.cpu().numpy()), 3)}
+        # roofline of the dominant kernel: step-2 block matching on the basic
+        # estimate (in the colour space the step sees), timed alone
+        b_ws = basic.clone()
+        vb.color_transform(b_ws, True)
+        n_dist = vb.bm_distance_count(b_ws, p2)
+        flops = bm_flops(p2.k, C, n_dist)
+        vb.similar_patches(b_ws, p2)
+        torch.cuda.synchronize()
+        bm_ms = timed(stream, lambda: vb.similar_patches(b_ws, p2), 3)
+        peak, peak_src = fp32_peak(dev, clocks)
+        achieved = flops / (bm_ms / 1e3) / 1e12
+        roofline = {"kernel": "bm2_kernel<7, 3> (step-2 block matching)", "bound": "fp32",
+                    "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                    "algorithmic_flops": flops, "distances": n_dist, "ms": round(bm_ms, 3)}
+        e2e = None
+        if args.e2e_steps > 0:
+            hn = torch.from_numpy(noisy).pin_memory().numpy()
+            hb = torch.empty(noisy.shape, dtype=torch.float32).pin_memory().numpy()
+            hf = torch.empty(noisy.shape, dtype=torch.float32).pin_memory().numpy()
+            vb.run_host(hn, SIGMA, p1, p2, color_space=COLOR, basic=hb, out=hf)
+            barrier(world)
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                vb.run_host(hn, SIGMA, p1, p2, color_space=COLOR, basic=hb, out=hf)
+            dt = reduce_max((time.perf_counter() - t0) / args.e2e_steps, world)
+            e2e = {"value": round(mpf * world / dt, 3), "unit": UNIT, "h2d_bytes_per_step": int(hn.nbytes),
+                   "d2h_bytes_per_step": int(hb.nbytes + hf.nbytes), "ms_per_step": round(dt * 1e3, 1)}
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            samples, desc = cpu_sample("1080p30", noisy=noisy)
+            val, th = time_cpu(samples)
+            cpu = {"value": round(val, 4), "unit": UNIT, "cores": th, "kind": "port",
+                   "sample": desc + ", %d OpenMP threads" % th}
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {"workload": WORKLOAD_1080, "global_batch": world,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (746 MB clip)", "quality": q},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": 10 * args.steps, "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
