@@ -70,23 +70,8 @@ def parse():
     return ap.parse_args()
 
 
-def batch_specs():
-    """(width, height, frames, channels, sigma) of the 64 clips."""
-    import numpy as np
-    rng = np.random.Generator(np.random.PCG64(4000))
-    out = []
-    for _ in range(64):
-        w = int(rng.integers(160, 1281))
-        h = int(rng.integers(120, 721))
-        f = int(rng.integers(5, 41))
-        c = int(rng.choice([1, 3]))
-        s = float(rng.choice([5, 10, 20, 30, 50]))
-        out.append((w, h, f, c, s))
-    return out
-
-
 def make_batch():
-    from vbm3d_gb300.synth import make_clip
+    from vbm3d_gb300.synth import batch_specs, make_clip
     clips = []
     for i, (w, h, f, c, s) in enumerate(batch_specs()):
         clean, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)

@@ -1,16 +1,26 @@
-"""One VBM3D run (both steps) on a seeded synthetic clip, for profilers.
+"""One VBM3D run (both steps) on seeded synthetic data, for profilers.
 
     python -m vbm3d_gb300.profile_case --width 1280 --height 720 --frames 16
+    python -m vbm3d_gb300.profile_case --batch 64 [--scale 0.5]
 
-Launch order inside one run (colour transform on): color, bm (step 1),
-filter<1>, normalize, bm (step 2), filter<2>, normalize, color x3.
+Plain form: one clip; launch order (colour transform on): color, bm (step
+1), filter<1>, normalize, bm (step 2), filter<2>, normalize, color x3.
+Batched form: the first `--batch` clips of the uneven-batch workload
+(synth.batch_specs, sides times `--scale`), one batch with a fixed
+configuration (no tuning pass), run once without the graph so that every
+kernel is its own launch (prep, block matching of step 1 per class,
+filtering of step 1 per table set, mid, the same for step 2, final), then
+once more through vbm3d_batch_profile, which prints each work launch.
 """
 import argparse
 
 import torch
 
 import vbm3d_gb300 as vb
-from vbm3d_gb300.synth import make_clip
+from vbm3d_gb300.synth import batch_specs, make_clip
+
+FIXED = dict(bm1_tile=4, bm1_warps=4, filter1_tile=16, filter1_warps=8, bm2_tile=8, bm2_warps=4, filter2_tile=16,
+             filter2_warps=8, no_graph=1)
 
 
 def main():
@@ -21,7 +31,23 @@ def main():
     ap.add_argument("--channels", type=int, default=3)
     ap.add_argument("--sigma", type=float, default=30.0)
     ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=0, help="batched form over this many clips")
+    ap.add_argument("--scale", type=float, default=1.0)
     a = ap.parse_args()
+    if a.batch:
+        clips = []
+        for i, (w, h, f, c, s) in enumerate(batch_specs(scale=a.scale)[:a.batch]):
+            _, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)
+            clips.append(dict(noisy=torch.from_numpy(noisy).cuda(), sigma=s))
+        b = vb.Batch(clips, color_space=True, config=FIXED)
+        for _ in range(a.runs):
+            b.run()
+        torch.cuda.synchronize()
+        for l in b.profile():
+            print("launch phase %d k %d C %d: %d clips, %d refs, %.2f ms" % (l["phase"], l["k"], l["channels"],
+                                                                            l["clips"], l["refs"], l["ms"]))
+        print("ok")
+        return
     _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
     x0 = torch.from_numpy(noisy).cuda()
     for _ in range(a.runs):

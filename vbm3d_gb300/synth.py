@@ -97,6 +97,24 @@ def make_clip(width, height, frames, channels, sigma, seed, vmax=3.0, with_flow=
     return clean, noisy.astype(np.float32), fflow, bflow
 
 
+def batch_specs(n=64, seed=4000, scale=1.0):
+    """(width, height, frames, channels, sigma) of the uneven-batch workload:
+    width uniform in 160-1280, height in 120-720, 5-40 frames, 1 or 3
+    channels, sigma in {5, 10, 20, 30, 50}, drawn from PCG64(seed); clip i
+    is generated with seed + i.  `scale` shrinks the sides (for small
+    profiling cases)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n):
+        w = int(rng.integers(160, 1281))
+        h = int(rng.integers(120, 721))
+        f = int(rng.integers(5, 41))
+        c = int(rng.choice([1, 3]))
+        s = float(rng.choice([5, 10, 20, 30, 50]))
+        out.append((max(16, int(w * scale)), max(16, int(h * scale)), f, c, s))
+    return out
+
+
 def psnr(clean, est):
     """PSNR with both videos clipped to [0, 255], as VideoUtils::computePSNR
     (src/Utilities/LibVideoT.hpp:576-597); computed in double."""
