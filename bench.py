@@ -251,10 +251,11 @@ def fp32_peak(dev, clocks):
 
 
 # DRAM bytes (read + write) per reference patch of the batched step-2 block
-# matching of RGB k = 7 clips, from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3> / its references) on
-# the profile case of vbm3d_gb300.profile_case --batch.
-BM2_DRAM_BYTES_PER_REF = None
+# matching of the RGB k = 7 clips: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3> on the full batch
+# (python -m vbm3d_gb300.profile_case --batch 64): 1.60 GB + 0.443 GB for
+# 12 308 991 reference patches.
+BM2_DRAM_BYTES_PER_REF = 166.0
 
 
 def timed(stream, fn, steps):
@@ -369,12 +370,14 @@ def run_gpu(args):
         flops = bm_flops(bm["k"], bm["channels"], n_dist)
         peak, peak_src = fp32_peak(dev, clocks)
         achieved = flops / (bm["ms"] / 1e3) / 1e12
-        traffic = None if BM2_DRAM_BYTES_PER_REF is None or (step, bm["k"], bm["channels"]) != (2, 7, 3) \
-            else BM2_DRAM_BYTES_PER_REF * bm["refs"]
+        traffic = BM2_DRAM_BYTES_PER_REF * bm["refs"] if (step, bm["k"], bm["channels"]) == (2, 7, 3) else None
         roofline = {"kernel": "batch_bm_kernel<%d, %d, %d> (step-%d block matching, %d clips)"
                               % (step, bm["k"], bm["channels"], step, bm["clips"]),
                     "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
-                    "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_src,
+                    "frac": round(achieved / peak, 4), "traffic": traffic,
+                    "traffic_source": "ncu DRAM bytes of this launch on the same workload, per reference patch "
+                                      "(profiles/batch_bm_kernel_step2_k7_rgb.md) x its reference patches",
+                    "peak_source": peak_src,
                     "algorithmic_flops": flops, "distances": n_dist, "refs": bm["refs"], "ms": round(bm["ms"], 2),
                     "share_of_run": round(bm["ms"] / sum(l["ms"] for l in launches), 3),
                     "largest_launch": "phase %d k=%d C=%d, %.1f ms" % (top["phase"], top["k"], top["channels"],
