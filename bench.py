@@ -375,8 +375,8 @@ def run_gpu(args):
                               % (step, bm["k"], bm["channels"], step, bm["clips"]),
                     "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                    "traffic_source": "ncu DRAM bytes of this launch on the same workload, per reference patch "
-                                      "(profiles/batch_bm_kernel_step2_k7_rgb.md) x its reference patches",
+                    "traffic_source": "ncu DRAM bytes (read + write) of this kernel on the full batch, per "
+                                      "reference patch, x the launch's reference patches",
                     "peak_source": peak_src,
                     "algorithmic_flops": flops, "distances": n_dist, "refs": bm["refs"], "ms": round(bm["ms"], 2),
                     "share_of_run": round(bm["ms"] / sum(l["ms"] for l in launches), 3),
