@@ -299,6 +299,7 @@ int build_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_spa
             P.invT[i * k + j] = P.inv[j * k + i];
         }
     P.bm_warp_bytes = bm_warp_bytes(P, P.bm_list_cap, P.bm_best_cap, P.bm_win_cap);
+    P.neg_zero = -0.0f;
     return VBM3D_OK;
 }
 

@@ -185,7 +185,8 @@ struct ClipHost {
 // One kernel launch of a work phase: the clips of one class.
 struct WorkLaunch {
     int phase = 0, cls = 0;
-    std::vector<int> clips;  // batch indices, in cost order
+    std::vector<int> clips;  // batch indices, in cost order; slot = position
+    std::vector<unsigned char> table;  // block matching: its BmTable, passed by value
     int ws = 0;              // per-warp workspace (bm: bytes, filter: floats)
     uint4* d_items = nullptr;
     unsigned nitems = 0;
@@ -252,14 +253,15 @@ std::vector<uint4> make_items(const vbm3d_batch& b, const WorkLaunch& w, int til
     std::vector<uint4> v;
     const int s = w.phase / 2;
     long long n = 0;
-    for (int c : w.clips) {
+    for (size_t slot = 0; slot < w.clips.size(); slot++) {
+        const int c = w.clips[slot];
         const StepHead& P = b.ch[c].h[s];
         const long long per_frame = (long long)P.nrows * P.ncols;
         for (int t = 0; t < P.nframes; t++)
             for (long long r = 0; r < per_frame; r += tile, n++)
                 if (n % stride == 0)
                     v.push_back(make_uint4((unsigned)c, (unsigned)(t * per_frame + r),
-                                           (unsigned)std::min<long long>(tile, per_frame - r), 0u));
+                                           (unsigned)std::min<long long>(tile, per_frame - r), (unsigned)slot));
     }
     return v;
 }
@@ -289,8 +291,7 @@ int upload_phase(vbm3d_batch& b, int phase, int tile, int stride, cudaStream_t s
 
 size_t launch_smem(const WorkLaunch& w, int warps)
 {
-    return (w.phase & 1) ? (size_t)(kViewFloats + warps * w.ws) * sizeof(float)
-                         : (size_t)(kHeadBytes + kLayoutBytes) + (size_t)warps * w.ws;
+    return (w.phase & 1) ? (size_t)(kViewFloats + warps * w.ws) * sizeof(float) : (size_t)warps * w.ws;
 }
 
 // Grid of a launch: resident blocks per SM x SMs.
@@ -324,7 +325,7 @@ cudaError_t launch_work(const vbm3d_batch& b, const WorkLaunch& w, int warps, un
     const uint4* items = w.d_items;
     unsigned n = w.nitems;
     int ws = w.ws;
-    void* args[] = {&clips, &items, &n, &h, &ws};
+    void* args[] = {&clips, &items, &n, &h, &ws, const_cast<unsigned char*>(w.table.data())};
     return cudaLaunchKernel(work_kernel(w.phase, w.cls), dim3(w.grid), dim3(warps * 32), args, launch_smem(w, warps),
                             s);
 }
@@ -492,6 +493,11 @@ void plan_launches(vbm3d_batch& b)
             for (int c : b.order) {
                 const StepHead& P = b.ch[c].h[s];
                 if (class_of(ph, P) != cls) continue;
+                if (!(ph & 1) && (int)w.clips.size() == kTableClips) {  // a full table: next launch
+                    b.work[ph].push_back(w);
+                    w.clips.clear();
+                    w.ws = 0;
+                }
                 w.clips.push_back(c);
                 if (ph & 1) w.ws = std::max(w.ws, (kMaxN + (s == 0 ? 1 : 2) * P.C * P.N * (P.k * P.k + 1) + 3) & ~3);
                 else w.ws = std::max(w.ws, (b.ch[c].L[s].warp_bytes + 15) & ~15);
@@ -602,6 +608,22 @@ int allocate(vbm3d_batch& b, cudaStream_t s)
         h.tab_idx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 3]);
         h.tab_nsx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 4]);
     }
+    // block-matching tables: parameters and buffers of each launch's clips
+    for (int ph = 0; ph < kPhases; ph += 2)
+        for (WorkLaunch& w : b.work[ph]) {
+            w.table.assign(sizeof(BmTable), 0);
+            BmTable* t = reinterpret_cast<BmTable*>(w.table.data());
+            for (size_t i = 0; i < w.clips.size(); i++) {
+                const int c = w.clips[i];
+                t->h[i] = b.ch[c].h[ph / 2];
+                t->L[i] = b.ch[c].L[ph / 2];
+                t->vid[i] = ph == 0 ? b.hc[c].y : b.hc[c].basic;
+                t->fflow[i] = b.hc[c].fflow;
+                t->bflow[i] = b.hc[c].bflow;
+                t->tab_idx[i] = b.hc[c].tab_idx;
+                t->tab_nsx[i] = b.hc[c].tab_nsx;
+            }
+        }
     BCK(cudaMalloc(&b.d_clips, b.hc.size() * sizeof(BatchClip)));
     BCK(cudaMemcpyAsync(b.d_clips, b.hc.data(), b.hc.size() * sizeof(BatchClip), cudaMemcpyHostToDevice, s));
     std::vector<uint4> ch;

@@ -46,16 +46,33 @@ struct BatchClip {
     unsigned wh, C, color, pad;
 };
 
-// Shared-memory copies of a clip's parameters at the start of a block's
-// dynamic shared memory (block matching: StepHead and Layout; filtering:
-// FilterView), 16-byte multiples.
-constexpr int kHeadBytes = (int)((sizeof(StepHead) + 15) & ~size_t(15));
-constexpr int kLayoutBytes = (int)((sizeof(Layout) + 15) & ~size_t(15));
+// The filtering kernels' shared-memory copy of a clip's FilterView at the
+// start of a block's dynamic shared memory, a 16-byte multiple.
 constexpr int kViewFloats = (int)(((sizeof(FilterView) + 15) & ~size_t(15)) / 4);
-static_assert(sizeof(StepHead) % 4 == 0 && sizeof(Layout) % 4 == 0 && sizeof(FilterView) % 4 == 0, "word copies");
+static_assert(sizeof(FilterView) % 4 == 0, "word copies");
 
-// A work item is a uint4 (clip, first reference, references, 0); the
-// references lie in one frame of the clip's grid.
+// Block matching reads its clips' parameters and buffers from a table
+// passed by value as a __grid_constant__ kernel argument (under the 32 KB
+// parameter limit), indexed by the work item's slot.  In parameter space
+// they are read through the constant cache and need no registers, as in
+// the plain kernel, whose parameters are kernel arguments too; copies in
+// shared memory or registers measured 10-40 % slower, the registers they
+// take being the ones the distance loop runs short of.
+constexpr int kTableClips = 150;
+struct BmTable {
+    StepHead h[kTableClips];
+    Layout L[kTableClips];
+    const float* vid[kTableClips];  // the video block matching reads
+    const float* fflow[kTableClips];
+    const float* bflow[kTableClips];
+    unsigned* tab_idx[kTableClips];
+    unsigned* tab_nsx[kTableClips];
+};
+static_assert(sizeof(BmTable) <= 31 * 1024, "kernel parameter limit");
+
+// A work item is a uint4 (clip, first reference, references, slot): the
+// references lie in one frame of the clip's grid; block matching reads
+// the clip's entries at `slot` of its launch's table.
 
 // Work phases and kernel classes: block matching has one class per
 // (k, C) in {7, 8} x {1, 3}; filtering one per transform table set,

@@ -38,45 +38,33 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // handle interleaved references of the tile (warp w: references w,
 // w + warps, ...), so at any time a block works on neighbouring reference
 // patches whose search windows and groups overlap in L1, as a block of the
-// plain kernel does.  A block keeps its current clip's parameters in
-// shared memory, reloaded when an item of another clip comes up.
+// plain kernel does.  Block matching reads its clips' parameters from the
+// launch's kernel-argument table (batch.cuh); filtering keeps its current
+// clip's parameters and tables in shared memory, reloaded when an item of
+// another clip comes up.
 
 template <int STEP, int K, int C>
 __global__ void __maxnreg__(C == 3 ? 96 : 80)  // as bm2_kernel
 batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
-                unsigned* __restrict__ head, int warp_bytes)
+                unsigned* __restrict__ head, int warp_bytes, const __grid_constant__ BmTable T)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint4 s_item[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    StepHead* P = reinterpret_cast<StepHead*>(smem);
-    Layout* L = reinterpret_cast<Layout*>(smem + kHeadBytes);
-    unsigned char* ws = smem + kHeadBytes + kLayoutBytes + (size_t)wid * warp_bytes;
-    unsigned cur = kNoItem;
+    unsigned char* ws = smem + (size_t)wid * warp_bytes;
     claim_item(items, nitems, head, &s_item[0]);
     __syncthreads();
     for (int buf = 0;; buf ^= 1) {
         const uint4 I = s_item[buf];
         if (I.x == kNoItem) break;
         claim_item(items, nitems, head, &s_item[buf ^ 1]);
-        const BatchClip& B = clips[I.x];
-        if (I.x != cur) {  // uniform over the block
-            copy_words(P, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
-            copy_words(L, &B.s[STEP - 1].L, (int)sizeof(Layout));
-            __syncthreads();
-            cur = I.x;
-        }
-        const float* vid = STEP == 1 ? B.y : B.basic;
+        const int t = (int)I.w;
         for (unsigned j = wid; j < I.z; j += nwarps) {
-            // register copies: the fields bm2_ref reads are loaded once per
-            // reference, not reloaded after each of its shared-memory stores
-            const StepHead Pr = *P;
-            const Layout Lr = *L;
-            bm2_ref<K, C>(Pr, Lr, (long long)I.y + j, ws, lane, vid, B.fflow, B.bflow, B.tab_idx, nullptr, nullptr,
-                          B.tab_nsx);
+            bm2_ref<K, C>(T.h[t], T.L[t], (long long)I.y + j, ws, lane, T.vid[t], T.fflow[t], T.bflow[t],
+                          T.tab_idx[t], nullptr, nullptr, T.tab_nsx[t]);
             __syncwarp();
         }
-        __syncthreads();  // publishes the next item; the parameters are reused
+        __syncthreads();  // publishes the next item
     }
 }
 

@@ -64,31 +64,29 @@ __host__ __device__ __forceinline__ int bm2_pitch(int s, int k)
 }
 
 // (a, b) += ((r, r) - (xa, xb))^2 with the rounding of the scalar
-// sequence d = r - x; s = s + d * d.  The subtraction and the accumulation
-// are packed f32x2 operations; the squares stay scalar multiplies, because
-// a packed multiply followed by a packed add is contracted into a fused
-// multiply-add below the PTX level (a GB300 probe found that pairing
-// changes the result in about half of all 192-term sums), whereas this
-// form reproduces the scalar sums bit for bit.
-__device__ __forceinline__ void sq_acc2(float& ax, float& ay, float rx, float ry, float xa, float xb)
+// sequence d = r - x; p = d * d; s = s + p.  Three packed f32x2
+// operations: subtract, square, add.  The square is fma(d, d, -0.0), which
+// rounds d * d once and adds an exact -0.0, so it equals the scalar
+// product in every case (including signed zeros).  A packed multiply
+// followed by a packed add is contracted into a fused multiply-add below
+// the PTX level (a GB300 probe found that pairing changes about half of all
+// 192-term sums), so the square must not be a plain multiply; `nz` is -0.0
+// read at run time, so that the compiler cannot turn the FMA into one.  A
+// GB300 probe found this form equal to the scalar sums in all of 65536
+// 192-term sums.
+__device__ __forceinline__ void sq_acc2(float& ax, float& ay, float rx, float ry, float xa, float xb, float nz)
 {
-    float dx, dy;
-    asm("{\n\t.reg .b64 r, x, d;\n\t"
+    asm("{\n\t.reg .b64 r, x, d, p, a, z;\n\t"
         "mov.b64 r, {%2, %3};\n\t"
         "mov.b64 x, {%4, %5};\n\t"
+        "mov.b64 z, {%6, %6};\n\t"
         "sub.rn.f32x2 d, r, x;\n\t"
-        "mov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(dx), "=f"(dy)
-        : "f"(rx), "f"(ry), "f"(xa), "f"(xb));
-    dx = __fmul_rn(dx, dx);
-    dy = __fmul_rn(dy, dy);
-    asm("{\n\t.reg .b64 a, d;\n\t"
+        "fma.rn.f32x2 p, d, d, z;\n\t"
         "mov.b64 a, {%0, %1};\n\t"
-        "mov.b64 d, {%2, %3};\n\t"
-        "add.rn.f32x2 a, a, d;\n\t"
+        "add.rn.f32x2 a, a, p;\n\t"
         "mov.b64 {%0, %1}, a;\n\t}"
         : "+f"(ax), "+f"(ay)
-        : "f"(dx), "f"(dy));
+        : "f"(rx), "f"(ry), "f"(xa), "f"(xb), "f"(nz));
 }
 
 struct Smem {
@@ -203,97 +201,127 @@ __device__ void small_partial_sort(Pair* a, int m, int n, int lane)
     __syncwarp();
 }
 
+// Float offset of the staged tile of window w of a phase whose tiles hold
+// tile_sz floats: windows are paired (0, 1), (2, 3), ..., and each pair
+// starts one float past a 32-float boundary after the previous one, so the
+// two pairs read by one pass fall on disjoint banks.
+__host__ __device__ __forceinline__ int bm2_pair_stride(int tile_sz) { return ((2 * tile_sz + 31) & ~31) + 1; }
+__host__ __device__ __forceinline__ int bm2_tile_offset(int w, int tile_sz)
+{
+    return (w >> 1) * bm2_pair_stride(tile_sz) + (w & 1) * tile_sz;
+}
+
+// Distances of every position of the phase's nw windows.  Windows are
+// taken in pairs (0, 1), (2, 3), ...; a lane owns one slot (dy, 2cx) of a
+// pair and evaluates positions (dy, 2cx) and (dy, 2cx + 1) of both windows
+// (4 candidates): per row of the patch it loads K + 1 staged pixels of
+// each window and the K reference pixels once, and the two windows share
+// each packed f32x2 operation.  An odd last window runs in passes of its
+// own, a lane evaluating positions (dy, 2cx) and (dy, 2cx + 1) of it as the
+// packed pair.  Every distance is the reference's sequential sum over
+// (c, hy, hx).
 template <int K, int C>
 __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
                                 int pitch, int plane)
 {
     constexpr int KK = K * K;
-    // pair windows (0,1), (2,3), ...; an odd last window is split in
-    // halves.  Each pair owns whole 32-lane rows of slots (slot j of a pair
-    // = position j of both windows), so one load instruction reads one tile
-    // and the rows of a window fall on distinct banks.
-    const int npairs = (nw + 1) / 2;
-    int rows_before[kMaxNb + 1];
-    int nrows = 0;
+    const int npairs = nw >> 1;
+    int pstart[kMaxNb + 1];
+    int total = 0;
 #pragma unroll
     for (int p = 0; p < kMaxNb; p++) {
-        rows_before[p] = nrows;
+        pstart[p] = total;
         if (p < npairs) {
-            const int wa = 2 * p, wb = 2 * p + 1;
-            const int na = npos(S.pw[wa]);
-            const int slots = wb < nw ? max(na, npos(S.pw[wb])) : (na + 1) / 2;
-            nrows += (slots + 31) >> 5;
+            const PWin& A = S.pw[2 * p];
+            const PWin& B = S.pw[2 * p + 1];
+            total += max(A.wh, B.wh) * ((max(A.ww, B.ww) + 1) >> 1);
         }
     }
-    rows_before[kMaxNb] = nrows;
+    pstart[kMaxNb] = total;
+    const int pair_passes = (total + 31) >> 5;
+    const int lone_slots = (nw & 1) ? S.pw[nw - 1].wh * ((S.pw[nw - 1].ww + 1) >> 1) : 0;
+    const int passes = pair_passes + ((lone_slots + 31) >> 5);
+    const float nz = P.neg_zero;
 
-    for (int rb = 0; rb < nrows; rb += 2) {
-        // two slot rows per pass; each slot carries two candidates
-        const float* tp[4];
+    for (int pass = 0; pass < passes; pass++) {
+        const bool pm = pass < pair_passes;  // uniform over the warp
+        const int sl = (pm ? pass : pass - pair_passes) * 32 + lane;
+        const float* tA = S.tiles;
+        const float* tB = S.tiles;
         int rslot[4], qxy[4], win[4];
-        bool valid[4];
+        bool valid[4] = {false, false, false, false};
+        {
+            int wa = nw - 1, wb = nw - 1, j = sl, limit = lone_slots;
+            if (pm) {
+                int p = 0;
 #pragma unroll
-        for (int s2 = 0; s2 < 2; s2++) {
-            const int row = rb + s2;
-            int p = 0;
+                for (int q = 1; q < kMaxNb; q++) p += (q < npairs && sl >= pstart[q]) ? 1 : 0;
+                wa = 2 * p;
+                wb = 2 * p + 1;
+                j = sl - pstart[p];
+                limit = total - pstart[p];
+                limit = p + 1 < npairs ? pstart[p + 1] - pstart[p] : limit;
+            }
+            if (j < limit) {
+                const PWin A = S.pw[wa];
+                const PWin B = S.pw[wb];
+                const int cp = (max(A.ww, B.ww) + 1) >> 1;
+                const int dy = pos_row(j, 1.0f / (float)cp), dx = 2 * (j - dy * cp);
+                tA = S.tiles + A.tile + dy * pitch + dx;
+                tB = S.tiles + B.tile + dy * pitch + dx;
+                // candidates: pairs (A dx, B dx, A dx+1, B dx+1); lone (A dx, A dx+1)
 #pragma unroll
-            for (int q = 1; q < kMaxNb; q++) p += (row >= rows_before[q] && q < npairs) ? 1 : 0;
-            const int j = ((row - rows_before[p]) << 5) + lane;
-            const int wa = 2 * p, wb = 2 * p + 1;
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int c4 = 2 * s2 + h;
-                valid[c4] = false;
-                tp[c4] = S.tiles;
-                win[c4] = 0;
-                rslot[c4] = 0;
-                qxy[c4] = 0;
-                if (row >= nrows) continue;
-                int w = wa, pos = j;
-                if (wb < nw) {
-                    w = h ? wb : wa;
-                } else {
-                    const int half = (npos(S.pw[wa]) + 1) / 2;
-                    if (j >= half) continue;
-                    if (h) pos = j + half;
-                }
-                const PWin pwn = S.pw[w];
-                if (pos < npos(pwn)) {
-                    const int dy = pos_row(pos, pwn.rcp_ww), dx = pos - dy * pwn.ww;
-                    valid[c4] = true;
-                    tp[c4] = S.tiles + pwn.tile + dy * pitch + dx;
-                    win[c4] = w;
-                    rslot[c4] = pwn.res + pos;
-                    qxy[c4] = ((pwn.y0 + dy) << 16) | (pwn.x0 + dx);
+                for (int q = 0; q < 4; q++) {
+                    const bool second = pm ? (q & 1) : false;
+                    const int w = second ? wb : wa;
+                    const PWin& W = second ? B : A;
+                    const int cx = dx + (pm ? (q >> 1) : q);
+                    valid[q] = (pm || q < 2) && dy < W.wh && cx < W.ww;
+                    win[q] = w;
+                    rslot[q] = W.res + dy * W.ww + cx;
+                    qxy[q] = ((W.y0 + dy) << 16) | (W.x0 + cx);
                 }
             }
         }
-        const bool two = __any_sync(kFull, valid[2] || valid[3]);
         float a0x = 0.f, a0y = 0.f, a1x = 0.f, a1y = 0.f;
+        if (pm) {
 #pragma unroll 1
-        for (int c = 0; c < C; c++) {
-            const float* t0 = tp[0] + c * plane;
-            const float* t1 = tp[1] + c * plane;
-            const float2* rr = S.refp + c * KK;
-            if (two) {
-                const float* t2 = tp[2] + c * plane;
-                const float* t3 = tp[3] + c * plane;
+            for (int c = 0; c < C; c++) {
+                const float* pa = tA + c * plane;
+                const float* pb = tB + c * plane;
+                const float2* rr = S.refp + c * KK;
 #pragma unroll 1
-                for (int hy = 0; hy < K; hy++)
+                for (int hy = 0; hy < K; hy++) {
+                    float va[K + 1], vb[K + 1];
+#pragma unroll
+                    for (int x = 0; x <= K; x++) {
+                        va[x] = pa[hy * pitch + x];
+                        vb[x] = pb[hy * pitch + x];
+                    }
 #pragma unroll
                     for (int hx = 0; hx < K; hx++) {
                         const float2 r2 = rr[hy * K + hx];
-                        sq_acc2(a0x, a0y, r2.x, r2.y, t0[hy * pitch + hx], t1[hy * pitch + hx]);
-                        sq_acc2(a1x, a1y, r2.x, r2.y, t2[hy * pitch + hx], t3[hy * pitch + hx]);
+                        sq_acc2(a0x, a0y, r2.x, r2.y, va[hx], vb[hx], nz);
+                        sq_acc2(a1x, a1y, r2.x, r2.y, va[hx + 1], vb[hx + 1], nz);
                     }
-            } else {
+                }
+            }
+        } else {
 #pragma unroll 1
-                for (int hy = 0; hy < K; hy++)
+            for (int c = 0; c < C; c++) {
+                const float* pa = tA + c * plane;
+                const float2* rr = S.refp + c * KK;
+#pragma unroll 1
+                for (int hy = 0; hy < K; hy++) {
+                    float va[K + 1];
+#pragma unroll
+                    for (int x = 0; x <= K; x++) va[x] = pa[hy * pitch + x];
 #pragma unroll
                     for (int hx = 0; hx < K; hx++) {
                         const float2 r2 = rr[hy * K + hx];
-                        sq_acc2(a0x, a0y, r2.x, r2.y, t0[hy * pitch + hx], t1[hy * pitch + hx]);
+                        sq_acc2(a0x, a0y, r2.x, r2.y, va[hx], va[hx + 1], nz);
                     }
+                }
             }
         }
         const float acc[4] = {a0x, a0y, a1x, a1y};
@@ -301,6 +329,7 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (!valid[q]) continue;
+            // pairs: q -> (a0x, a0y, a1x, a1y); lone: q 0, 1 -> (a0x, a0y)
             const PWin& pwn = S.pw[win[q]];
             const int qx = qxy[q] & 0xffff, qy = qxy[q] >> 16;
             // seen: inside an earlier window on the same frame
@@ -496,7 +525,7 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
                 const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
                 py = min(max((int)((float)py + roundf(fy)), 0), P.H - K);
                 w = make_window(P, chain == 1 ? pt + 1 : pt - 1, px, py, P.Npr, chain);
-                w.tile = lane * tile_sz;
+                w.tile = bm2_tile_offset(lane, tile_sz);
                 n = npos(w);
             }
             // exclusive prefix sum of the window sizes: result offsets
@@ -597,7 +626,9 @@ inline Layout bm2_layout(const StepHead& P)
           P.H <= 8192 && P.Nf <= 16))
         return L;
     const int p0 = bm2_pitch(P.Ns, P.k), p1 = bm2_pitch(P.Npr, P.k);
-    L.tile_floats = max(P.C * p0 * (P.Ns + P.k - 1), 2 * P.Nb * P.C * p1 * (P.Npr + P.k - 1));
+    // phase 0: one Ns window; phase f: up to 2 Nb Npr windows in pairs; plus
+    // the one-column over-read of the last slot of an odd-width window
+    L.tile_floats = max(P.C * p0 * (P.Ns + P.k - 1), P.Nb * bm2_pair_stride(P.C * p1 * (P.Npr + P.k - 1))) + 8;
     L.tile_floats = (L.tile_floats + 3) & ~3;
     L.res_cap = max(max(P.Ns * P.Ns, 2 * P.Nb * P.Npr * P.Npr), P.Nb * (1 + 2 * P.Nf));
     L.scr_cap = max(P.Ns * P.Ns, P.Npr * P.Npr);

@@ -58,6 +58,9 @@ struct StepHead {
     float sigma[kMaxC];
     // block-matching shared-memory layout (floats / pairs per warp)
     int bm_list_cap, bm_best_cap, bm_win_cap, bm_warp_bytes;
+    // -0.0f, read by the kernels at run time (the addend of the exact
+    // squaring FMA of block matching, which must not be a constant)
+    float neg_zero;
 };
 
 // Transform tables of a step (k*k each, row-major, row stride k).
