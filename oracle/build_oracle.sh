@@ -8,3 +8,5 @@ gcc -std=c99 -O2 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared \
     -I"$HERE" -I"$HERE/fftw_shim" \
     "$HERE/vbm3d_oracle.c" "$HERE/fftw_shim/fftw_shim.c" -lm \
     -o "$HERE/_build/liboracle.so"
+gcc -std=c99 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -I"$HERE" \
+    "$HERE/tvl1_oracle.c" -lm -o "$HERE/_build/libtvl1_oracle.so"

@@ -8,6 +8,9 @@
 #   oracle/_ref/libvbm3d_ref_fast.so   the reference's CMake flags
 #       (-O3 -ffast-math -fomit-frame-pointer, CMakeLists.txt:15) + OpenMP:
 #       the reference as shipped, for the noise floor and CPU timing
+#   oracle/_ref/libtvl1_ref.so   the reference's TV-L1 library
+#       (tvl1flow/tvl1flow_lib.c and the files it includes), single thread,
+#       no FP contraction: the pin of the TV-L1 restatement
 # FFTW3f is not installed: oracle/fftw_shim supplies REDFT10/REDFT01.
 set -e
 REF=${1:-/root/reference}
@@ -31,4 +34,6 @@ build() {
 }
 build libvbm3d_ref_exact.so -O2 -ffp-contract=off -fno-fast-math
 build libvbm3d_ref_fast.so -O3 -ffast-math -fomit-frame-pointer
+gcc -std=c99 -w -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -I"$REF/tvl1flow" \
+    "$HERE/ref_harness/tvl1_ref_harness.c" -lm -o "$OUT/libtvl1_ref.so"
 echo "built $OUT"

@@ -216,3 +216,78 @@ class RefLib:
                               int(color_space), dims_of(nz), threads)
         assert rc == 0, rc
         return basic, den
+
+
+TVL1_ORACLE_SO = os.path.join(HERE, "_build", "libtvl1_oracle.so")
+TVL1_REF_SO = os.path.join(HERE, "_ref", "libtvl1_ref.so")
+
+
+class TvParams(C.Structure):
+    """tv_params of oracle/tvl1_oracle.h (the reference's TV-L1 options)."""
+    _fields_ = [("tau", C.c_float), ("lambda_", C.c_float), ("theta", C.c_float), ("nscales", C.c_int),
+                ("fscale", C.c_int), ("zfactor", C.c_float), ("nwarps", C.c_int), ("epsilon", C.c_float)]
+
+
+class TvlOracle:
+    """The C restatement of the reference's TV-L1 optical flow
+    (oracle/tvl1_oracle.c)."""
+
+    def __init__(self, path=TVL1_ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle()
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.tv_default_params.argtypes = [C.POINTER(TvParams)]
+        L.tv_flow.argtypes = [_fp, _fp, C.c_int, C.c_int, C.POINTER(TvParams), _fp, C.POINTER(C.c_int)]
+        L.tv_scales.argtypes = [C.c_int, C.c_int, C.POINTER(TvParams), C.POINTER(C.c_int)]
+
+    def default_params(self, **kw):
+        p = TvParams()
+        self.lib.tv_default_params(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, "lambda_" if k == "lambda" else k, v)
+        return p
+
+    def scales(self, nx, ny, p):
+        fs = C.c_int(0)
+        return self.lib.tv_scales(nx, ny, C.byref(p), C.byref(fs)), fs.value
+
+    def flow(self, I0, I1, p=None, iters=False):
+        """Flow [2, H, W] from I0 to I1 ([H, W] float32); with iters, also the
+        iteration counts [nscales, nwarps] (-1 below fscale)."""
+        p = p or self.default_params()
+        I0 = np.ascontiguousarray(I0, np.float32)
+        I1 = np.ascontiguousarray(I1, np.float32)
+        ny, nx = I0.shape
+        out = np.zeros((2, ny, nx), np.float32)
+        ns, _ = self.scales(nx, ny, p)
+        it = np.zeros((max(ns, 1), p.nwarps), np.int32)
+        rc = self.lib.tv_flow(_f(I0), _f(I1), nx, ny, C.byref(p), _f(out), it.ctypes.data_as(C.POINTER(C.c_int)))
+        if rc:
+            raise ValueError("tv_flow failed")
+        return (out, it) if iters else out
+
+
+class TvlRef:
+    """The reference's own TV-L1 library compiled from its sources
+    (oracle/_ref/libtvl1_ref.so; present only where the sources were)."""
+
+    def __init__(self):
+        if not os.path.exists(TVL1_REF_SO):
+            raise FileNotFoundError(TVL1_REF_SO)
+        self.lib = C.CDLL(TVL1_REF_SO)
+        self.lib.ref_tvl1_flow.argtypes = [_fp, _fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                                           C.c_int, C.c_float, C.c_int, C.c_float, _fp]
+
+    @staticmethod
+    def available():
+        return os.path.exists(TVL1_REF_SO)
+
+    def flow(self, I0, I1, p):
+        I0 = np.ascontiguousarray(I0, np.float32).copy()  # the reference's signature is not const
+        I1 = np.ascontiguousarray(I1, np.float32).copy()
+        ny, nx = I0.shape
+        out = np.zeros((2, ny, nx), np.float32)
+        self.lib.ref_tvl1_flow(_f(I0), _f(I1), nx, ny, p.tau, p.lambda_, p.theta, p.nscales, p.fscale, p.zfactor,
+                               p.nwarps, p.epsilon, _f(out))
+        return out
