@@ -276,6 +276,48 @@ int vbm3d_batch_get_config(const vbm3d_batch *batch, vbm3d_batch_config *config)
 int vbm3d_batch_profile(vbm3d_batch *batch, void *stream, vbm3d_batch_launch *out, int cap, int *count);
 void vbm3d_batch_destroy(vbm3d_batch *batch);
 
+/* TV-L1 optical flow: the flows the block matching's predictive search
+ * reads, which the reference computes on the CPU with tvl1flow
+ * (Dual_TVL1_optic_flow_multiscale, tvl1flow/tvl1flow_lib.c:356-488, after
+ * image_normalization, with the scale count of tvl1flow/main.c:151-157).
+ * Options mirror tvl1flow's command line (tvl1flow/main.c:84-96). */
+typedef struct vbm3d_tvl1_params {
+    float tau;       /* time step, (0, 0.25] */
+    float lambda;    /* data-term weight */
+    float theta;     /* tightness */
+    int nscales;     /* maximum number of scales */
+    int fscale;      /* finest scale computed (finer ones are upsampled) */
+    float zfactor;   /* pyramid factor, (0, 1) */
+    int nwarps;      /* warpings per scale */
+    float epsilon;   /* stopping threshold */
+} vbm3d_tvl1_params;
+
+/* The options the reference's flow scripts pass (tvl1flow/tvl1flow_forward.sh,
+ * tvl1flow_backward.sh: 0.25 0.2 0.3 100 2 0.5 5 0.01). */
+int vbm3d_tvl1_default_params(vbm3d_tvl1_params *params);
+
+/* Scales used for a width x height image (tvl1flow/main.c:151-157). */
+int vbm3d_tvl1_scales(unsigned width, unsigned height, const vbm3d_tvl1_params *params,
+                      int *nscales, int *fscale);
+
+/* Flows of `npairs` frame pairs: I0 and I1 hold npairs one-channel frames
+ * each ([npairs][H][W], device), flow receives [npairs][2][H][W] (x then y
+ * component, the motion from I0 to I1).  iterations: NULL, or HOST
+ * int[npairs][nscales][nwarps] for the iteration count of every warping (-1
+ * for scales below fscale).  Synchronises `stream`. */
+int vbm3d_gpu_tvl1_pairs(const float *I0, const float *I1, unsigned npairs, unsigned width,
+                         unsigned height, const vbm3d_tvl1_params *params, float *flow,
+                         int *iterations, void *stream);
+
+/* Forward and backward flows of a one-channel video ([F][H][W], device) in
+ * the layout the steps read (see the top of this file): fflow[t] = flow of
+ * frame t -> t+1, bflow[t] = flow of frame t+1 -> t, the last frame's
+ * entries zero; what tvl1flow_forward.sh / tvl1flow_backward.sh compute frame
+ * pair by frame pair.  All 2 (F - 1) pairs run together.  Synchronises
+ * `stream`. */
+int vbm3d_gpu_tvl1_video(const float *video, unsigned width, unsigned height, unsigned frames,
+                         const vbm3d_tvl1_params *params, float *fflow, float *bflow, void *stream);
+
 /* Measurement helper with no reference counterpart: runs the block
  * matching of vbm3d_gpu_similar_patches and returns in *count the total
  * number of patch distances it evaluated (calls of the reference's

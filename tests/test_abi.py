@@ -139,3 +139,22 @@ def test_batch_rejects_bad_clips_before_any_cuda_call(lib):
     bad = BatchConfig(bm1_tile=4)
     assert lib.vbm3d_batch_create(clips, 2, 1, C.byref(bad), C.byref(h), None) == 1
     assert not h.value
+
+
+def test_tvl1_rejects_bad_options_before_any_cuda_call(lib):
+    from vbm3d_gb300._abi import TvParams
+    p = TvParams()
+    assert lib.vbm3d_tvl1_default_params(C.byref(p)) == 0
+    assert (p.tau, p.lambda_, p.theta, p.nscales, p.fscale, p.zfactor, p.nwarps) == (
+        0.25, np.float32(0.2), np.float32(0.3), 100, 2, 0.5, 5)
+    ns, fs = C.c_int(), C.c_int()
+    assert lib.vbm3d_tvl1_scales(960, 540, C.byref(p), C.byref(ns), C.byref(fs)) == 0 and (ns.value, fs.value) == (7, 2)
+    fake = C.c_void_p(16)
+    for bad in (dict(tau=0.3), dict(zfactor=1.0), dict(nwarps=0), dict(epsilon=0.0), dict(lambda_=-1.0)):
+        q = TvParams()
+        lib.vbm3d_tvl1_default_params(C.byref(q))
+        for k, v in bad.items():
+            setattr(q, k, v)
+        assert lib.vbm3d_gpu_tvl1_pairs(fake, fake, 1, 64, 48, C.byref(q), fake, None, None) == 1
+    assert lib.vbm3d_gpu_tvl1_pairs(fake, fake, 0, 64, 48, C.byref(p), fake, None, None) == 1
+    assert lib.vbm3d_gpu_tvl1_video(fake, 64, 48, 1, C.byref(p), fake, fake, None) == 1

@@ -12,6 +12,7 @@ Entry points mirror the reference's hot path (tehret/vbm3d):
   normalize(...)                     run_vbm3d's num/den division (src/vbm3d.cpp:168-202)
   color_transform(...)               VideoUtils::transformColorSpace
   similar_patches(...)               computeSimilarPatches over the reference grid
+  tvl1_flow(...), tvl1_video(...)    tvl1flow's TV-L1 (Dual_TVL1_optic_flow_multiscale), frame pairs / a clip
   run(...) / run_host(...)           run_vbm3d (src/vbm3d.cpp:87-376), device / host buffers
 Beside them, with no reference counterpart:
   Batch(...)                         many uneven clips in one CUDA graph (vbm3d_batch_*)
@@ -21,7 +22,7 @@ import ctypes as C
 import os
 
 from ._abi import (BIOR, DCT, HAAR, HADAMARD, STATUS, BatchConfig, BatchLaunch, Clip, Dims,  # noqa: F401
-                   Params, dims_of)
+                   Params, TvParams, dims_of)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libvbm3d_gb300.so")
@@ -70,6 +71,11 @@ def load(path=LIB_PATH):
     L.vbm3d_batch_profile.argtypes = [vp, vp, C.POINTER(BatchLaunch), C.c_int, C.POINTER(C.c_int)]
     L.vbm3d_batch_destroy.argtypes = [vp]
     L.vbm3d_batch_destroy.restype = None
+    T = C.POINTER(TvParams)
+    L.vbm3d_tvl1_default_params.argtypes = [T]
+    L.vbm3d_tvl1_scales.argtypes = [C.c_uint, C.c_uint, T, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.vbm3d_gpu_tvl1_pairs.argtypes = [vp, vp, C.c_uint, C.c_uint, C.c_uint, T, vp, C.POINTER(C.c_int), vp]
+    L.vbm3d_gpu_tvl1_video.argtypes = [vp, C.c_uint, C.c_uint, C.c_uint, T, vp, vp, vp]
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -222,6 +228,56 @@ class LinearStep:
             self.close()
         except Exception:
             pass
+
+
+def tvl1_params(**kw):
+    """TV-L1 options: the reference's flow-script values, with overrides
+    (tau, lambda_, theta, nscales, fscale, zfactor, nwarps, epsilon)."""
+    p = TvParams()
+    _check(load().vbm3d_tvl1_default_params(C.byref(p)))
+    for k, v in kw.items():
+        setattr(p, "lambda_" if k == "lambda" else k, v)
+    return p
+
+
+def tvl1_flow(I0, I1, params=None, iterations=False, stream=None):
+    """TV-L1 flows from I0 to I1: CUDA float32 [P, H, W] (or [H, W]) frames;
+    returns [P, 2, H, W] (or [2, H, W]); with iterations, also the host
+    counts [P, nscales, nwarps]."""
+    import numpy as np
+    import torch
+    params = params or tvl1_params()
+    single = I0.dim() == 2
+    if single:
+        I0, I1 = I0[None], I1[None]
+    if not (I0.is_cuda and I0.dtype == torch.float32 and I0.is_contiguous() and I1.shape == I0.shape
+            and I1.is_contiguous() and I1.dtype == torch.float32):
+        raise TypeError("I0, I1 must be contiguous float32 CUDA tensors of one shape [P, H, W]")
+    npairs, h, w = I0.shape
+    flow = torch.empty((npairs, 2, h, w), dtype=torch.float32, device=I0.device)
+    ns, fs = C.c_int(0), C.c_int(0)
+    _check(load().vbm3d_tvl1_scales(w, h, C.byref(params), C.byref(ns), C.byref(fs)))
+    it = np.zeros((npairs, max(ns.value, 1), params.nwarps), np.int32) if iterations else None
+    _check(load().vbm3d_gpu_tvl1_pairs(_ptr(I0), _ptr(I1), npairs, w, h, C.byref(params), _ptr(flow),
+                                       None if it is None else it.ctypes.data_as(C.POINTER(C.c_int)),
+                                       _stream(stream)))
+    out = flow[0] if single else flow
+    return (out, it) if iterations else out
+
+
+def tvl1_video(video, params=None, stream=None):
+    """Forward and backward TV-L1 flows of a one-channel clip (CUDA float32
+    [F, H, W]) in the layout the steps read: (fflow, bflow), each
+    [F, 2, H, W]."""
+    import torch
+    params = params or tvl1_params()
+    if not (video.is_cuda and video.dtype == torch.float32 and video.is_contiguous() and video.dim() == 3):
+        raise TypeError("video must be a contiguous float32 CUDA tensor [F, H, W]")
+    f, h, w = video.shape
+    ff = torch.empty((f, 2, h, w), dtype=torch.float32, device=video.device)
+    bf = torch.empty_like(ff)
+    _check(load().vbm3d_gpu_tvl1_video(_ptr(video), w, h, f, C.byref(params), _ptr(ff), _ptr(bf), _stream(stream)))
+    return ff, bf
 
 
 class Batch:

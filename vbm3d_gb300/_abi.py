@@ -86,3 +86,9 @@ class BatchLaunch(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class TvParams(C.Structure):
+    """vbm3d_tvl1_params: TV-L1 options (tvl1flow's command line)."""
+    _fields_ = [("tau", C.c_float), ("lambda_", C.c_float), ("theta", C.c_float), ("nscales", C.c_int),
+                ("fscale", C.c_int), ("zfactor", C.c_float), ("nwarps", C.c_int), ("epsilon", C.c_float)]
