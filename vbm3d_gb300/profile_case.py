@@ -2,6 +2,7 @@
 
     python -m vbm3d_gb300.profile_case --width 1280 --height 720 --frames 16
     python -m vbm3d_gb300.profile_case --batch 64 [--scale 0.5]
+    python -m vbm3d_gb300.profile_case --tvl1 --width 960 --height 540 --frames 16
 
 Plain form: one clip; launch order (colour transform on): color, bm (step
 1), filter<1>, normalize, bm (step 2), filter<2>, normalize, color x3.
@@ -11,6 +12,8 @@ configuration (no tuning pass), run once without the graph so that every
 kernel is its own launch (prep, block matching of step 1 per class,
 filtering of step 1 per table set, mid, the same for step 2, final), then
 once more through vbm3d_batch_profile, which prints each work launch.
+TV-L1: forward and backward flows of a one-channel clip with the options of
+the reference's flow scripts (vbm3d_gpu_tvl1_video), run twice.
 """
 import argparse
 
@@ -33,7 +36,16 @@ def main():
     ap.add_argument("--runs", type=int, default=1)
     ap.add_argument("--batch", type=int, default=0, help="batched form over this many clips")
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--tvl1", action="store_true", help="TV-L1 flows of a one-channel clip")
     a = ap.parse_args()
+    if a.tvl1:
+        _, noisy, _, _ = make_clip(a.width, a.height, a.frames, 1, a.sigma, seed=4000, vmax=6.0)
+        v = torch.from_numpy(noisy[:, 0].copy()).cuda()
+        for _ in range(2):
+            vb.tvl1_video(v)
+        torch.cuda.synchronize()
+        print("ok")
+        return
     if a.batch:
         clips = []
         for i, (w, h, f, c, s) in enumerate(batch_specs(scale=a.scale)[:a.batch]):
