@@ -361,12 +361,6 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
 
 // Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
 // channels, at tile pitch `pitch`.
-// 4-byte asynchronous global -> shared copy (no register round trip).
-__device__ __forceinline__ void cp_async4(float* dst, const float* src)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-}
 
 template <int K, int C>
 __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, int lane,

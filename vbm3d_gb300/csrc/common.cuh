@@ -160,6 +160,16 @@ __device__ __forceinline__ void color3(float& a, float& b, float& c, bool forwar
     }
 }
 
+// 4-byte asynchronous global -> shared copy (no register round trip), and
+// the wait for all of the calling thread's copies; after the wait, a
+// __syncwarp makes every lane's copies visible to the warp.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 struct Pair {
     float d;
     unsigned i;

@@ -191,7 +191,10 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepHead& P, const T
 // Gathers the nsx patches of every channel into slices [c][n][K*K] of
 // stride SS, lanes over consecutive pixels (each patch row is contiguous in
 // memory, so a warp load touches a few rows instead of 32 patches).  idx[n]
-// is the patch's linear index in channel 0; log2n = log2(nsx).
+// is the patch's linear index in channel 0; log2n = log2(nsx).  The copies
+// are asynchronous (cp.async): the caller waits for them with
+// cp_async_wait_all() and a __syncwarp before reading the slices, so that
+// the gathers of one group (and of a second video) are in flight together.
 template <int K, int SS>
 __device__ __forceinline__ void gather_k(const StepHead& P, const float* __restrict__ vid, const unsigned* idx,
                                          int nsx, int log2n, float* g, int lane)
@@ -202,7 +205,7 @@ __device__ __forceinline__ void gather_k(const StepHead& P, const float* __restr
         const int sl = e / K2, pq = e - sl * K2;
         const int c = sl >> log2n, n = sl & (nsx - 1);
         const int p = pq / K, q = pq - p * K;
-        g[sl * SS + pq] = __ldg(vid + idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q);
+        cp_async4(g + sl * SS + pq, vid + idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q);
     }
 }
 
@@ -369,6 +372,7 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
 
     gather_k<K, SS>(P, noisy, idx, nsx, log2n, gA, lane);
     if (STEP == 2) gather_k<K, SS>(P, basic, idx, nsx, log2n, gB, lane);
+    cp_async_wait_all();
     __syncwarp();
     // 2D transforms, one slice (c, n) per lane, in registers
     slice_fwd<K, SS>(P, T, gA, nsl, lane);

@@ -221,6 +221,7 @@ linear_kernel(const StepParams P, const float* __restrict__ src, const float* __
     const int nsl = C * nsx;
 
     gather_k<K, SS>(P, src, idx, nsx, log2n, gS, lane);
+    cp_async_wait_all();
     __syncwarp();
     for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gS + sl * SS, P, P);
     __syncwarp();
@@ -229,6 +230,7 @@ linear_kernel(const StepParams P, const float* __restrict__ src, const float* __
 
     if (!ADJ) {
         gather_k<K, SS>(P, x, idx, nsx, log2n, gX, lane);
+        cp_async_wait_all();
         __syncwarp();
         for (int sl = lane; sl < nsl; sl += 32) slice_fwd2d<K>(gX + sl * SS, P, P);
         __syncwarp();
