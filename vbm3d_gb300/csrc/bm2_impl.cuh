@@ -107,6 +107,34 @@ __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) &
 // Number of positions of a window.
 __device__ __forceinline__ int npos(const PWin& w) { return w.ww * w.wh; }
 
+// The m smallest valid entries of res[0..n) (scan order), sorted into
+// out[0..m) by the restatement of the reference's partial_sort on lane 0:
+// the order among equal distances that std::partial_sort leaves.
+__device__ void tie_fallback(const Pair* res, int n, int m, int lane, Pair* out, Pair* scratch)
+{
+    __syncwarp();
+    if (lane == 0) {
+        int k = 0;
+        for (int j = 0; j < n; j++)
+            if (res[j].i != kNone) scratch[k++] = res[j];
+        partial_sort(scratch, m, k);
+        for (int r = 0; r < m; r++) out[r] = scratch[r];
+    }
+}
+
+// An unsigned key with the order of the distance d (never NaN or -0 here:
+// sums of squares from +0, less a bias), and back.
+__device__ __forceinline__ unsigned dist_key(float d)
+{
+    const unsigned u = __float_as_uint(d);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_dist(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+constexpr unsigned kNoKey = 0xffffffffu;  // above every distance's key
+
 // Top-min(Nb, #valid) of window w (distances in S.res[w.res ...], scan
 // order), appended sorted to out[*nout]: localSearch's partial_sort
 // (src/vbm3d.cpp:1075-1079).
@@ -115,6 +143,41 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
 {
     const int n = npos(w);
     const Pair* res = S.res + w.res;
+    if (n <= 64) {
+        // up to two entries per lane, as keys: each rank is one warp
+        // minimum, and a rank held by two entries is a tie
+        unsigned k0 = kNoKey, k1 = kNoKey, i0 = 0, i1 = 0;
+        if (lane < n) {
+            const Pair e = res[lane];
+            if (e.i != kNone) k0 = dist_key(e.d), i0 = e.i;
+        }
+        if (lane + 32 < n) {
+            const Pair e = res[lane + 32];
+            if (e.i != kNone) k1 = dist_key(e.d), i1 = e.i;
+        }
+        const unsigned mine = (k0 != kNoKey ? 1u : 0u) + (k1 != kNoKey ? 1u : 0u);
+        const int m = min(P.Nb, (int)__reduce_add_sync(kFull, mine));
+        bool tie = false;
+        for (int r = 0; r < m; r++) {
+            const unsigned wmin = __reduce_min_sync(kFull, min(k0, k1));
+            const unsigned c = (k0 == wmin ? 1u : 0u) + (k1 == wmin ? 1u : 0u);
+            if (__reduce_add_sync(kFull, c) != 1u) {
+                tie = true;
+                break;
+            }
+            if (k0 == wmin) {
+                out[nout + r] = Pair{key_dist(wmin), i0};
+                k0 = kNoKey;
+            } else if (k1 == wmin) {
+                out[nout + r] = Pair{key_dist(wmin), i1};
+                k1 = kNoKey;
+            }
+        }
+        if (tie) tie_fallback(res, n, m, lane, out + nout, scratch);
+        nout += m;
+        __syncwarp();
+        return;
+    }
     int nvalid = 0;
     for (int j0 = 0; j0 < n; j0 += 32) {
         const int j = j0 + lane;
@@ -154,16 +217,7 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
         if (lane == 0) out[nout + r] = res[wj];
         last = wmin;
     }
-    if (tie) {
-        __syncwarp();
-        if (lane == 0) {
-            int k = 0;
-            for (int j = 0; j < n; j++)
-                if (res[j].i != kNone) scratch[k++] = res[j];
-            partial_sort(scratch, m, k);
-            for (int r = 0; r < m; r++) out[nout + r] = scratch[r];
-        }
-    }
+    if (tie) tie_fallback(res, n, m, lane, out + nout, scratch);
     nout += m;
     __syncwarp();
 }
