@@ -122,18 +122,24 @@ __device__ void tie_fallback(const Pair* res, int n, int m, int lane, Pair* out,
     }
 }
 
-// An unsigned key with the order of the distance d (never NaN or -0 here:
-// sums of squares from +0, less a bias), and back.
+constexpr unsigned kNoKey = 0xffffffffu;   // no entry: above every key
+constexpr unsigned kNanKey = 0xfffffffeu;  // a NaN distance (from NaN or Inf pixels): above every number
+
+// An unsigned key with the order of the distance d under float
+// comparison (-0 ranks with +0; every NaN is kNanKey), and back (-0 comes
+// back as +0, which no distance here is: sums of squares from +0, less a
+// bias).
 __device__ __forceinline__ unsigned dist_key(float d)
 {
-    const unsigned u = __float_as_uint(d);
+    unsigned u = __float_as_uint(d);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return kNanKey;
+    if (u == 0x80000000u) u = 0u;
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 __device__ __forceinline__ float key_dist(unsigned k)
 {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
-constexpr unsigned kNoKey = 0xffffffffu;  // above every distance's key
 
 // Top-min(Nb, #valid) of window w (distances in S.res[w.res ...], scan
 // order), appended sorted to out[*nout]: localSearch's partial_sort
@@ -145,7 +151,10 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
     const Pair* res = S.res + w.res;
     if (n <= 64) {
         // up to two entries per lane, as keys: each rank is one warp
-        // minimum, and a rank held by two entries is a tie
+        // minimum, and a rank held by two entries is a tie.  Every valid
+        // entry counts towards m and has a key below kNoKey, so each of
+        // the m ranks finds one; a NaN at a rank goes to the restatement
+        // of partial_sort, as a tie does
         unsigned k0 = kNoKey, k1 = kNoKey, i0 = 0, i1 = 0;
         if (lane < n) {
             const Pair e = res[lane];
@@ -161,7 +170,7 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
         for (int r = 0; r < m; r++) {
             const unsigned wmin = __reduce_min_sync(kFull, min(k0, k1));
             const unsigned c = (k0 == wmin ? 1u : 0u) + (k1 == wmin ? 1u : 0u);
-            if (__reduce_add_sync(kFull, c) != 1u) {
+            if (wmin == kNanKey || __reduce_add_sync(kFull, c) != 1u) {
                 tie = true;
                 break;
             }
@@ -421,20 +430,25 @@ __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __res
                             int pitch, int plane)
 {
     // every tile row of every window is copied asynchronously, then waited
-    // for once: the loads of the whole phase are in flight together
+    // for once: the loads of the whole phase are in flight together.  The
+    // clip's geometry is read into registers before the first copy.
+    const long long W = P.W, wh = P.wh, whc = P.whc;
+    const unsigned tiles = smem_addr(S.tiles);
     for (int w = 0; w < nw; w++) {
         const PWin pwn = S.pw[w];
         const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
-        const float* src = vid + (size_t)pwn.t * P.whc + (size_t)pwn.y0 * P.W + pwn.x0;
-        float* dst = S.tiles + pwn.tile;
         const int x = tw <= 16 ? (lane & 15) : lane, ystep = tw <= 16 ? 2 : 1, y0 = tw <= 16 ? (lane >> 4) : 0;
         if (x < tw) {
+            const float* src = vid + pwn.t * whc + (pwn.y0 + y0) * W + pwn.x0 + x;
+            const unsigned dst = tiles + 4u * (unsigned)(pwn.tile + y0 * pitch + x);
+            const long long sstep = ystep * W;
+            const unsigned dstep = 4u * (unsigned)(ystep * pitch);
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
-                const float* sc = src + (size_t)c * P.wh + x;
-                float* dc = dst + c * plane + x;
+                const float* s = src + c * wh;
+                unsigned d = dst + 4u * (unsigned)(c * plane);
 #pragma unroll 4
-                for (int y = y0; y < th; y += ystep) cp_async4(dc + y * pitch, sc + (size_t)y * P.W);
+                for (int y = y0; y < th; y += ystep, s += sstep, d += dstep) cp_async4s(d, s);
             }
         }
     }

@@ -160,13 +160,16 @@ __device__ __forceinline__ void color3(float& a, float& b, float& c, bool forwar
     }
 }
 
-// 4-byte asynchronous global -> shared copy (no register round trip), and
-// the wait for all of the calling thread's copies; after the wait, a
-// __syncwarp makes every lane's copies visible to the warp.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+// 4-byte asynchronous global -> shared copy (no register round trip) to a
+// shared-window address (smem_addr), and the wait for all of the calling
+// thread's copies; after the wait, a __syncwarp makes every lane's copies
+// visible to the warp.  The "memory" clobber of every copy makes the
+// compiler reload values that live in memory (kernel parameters included)
+// after it, so callers keep what a copy loop needs in registers.
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async4s(unsigned dst, const float* src)
 {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 

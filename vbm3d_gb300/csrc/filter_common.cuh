@@ -82,7 +82,10 @@ template <bool PAIR>
 __device__ __forceinline__ void agg_add(const AggTarget& A, size_t o, float v, float kw)
 {
     if (PAIR) {
-        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(A.pair + 2 * o), "f"(v), "f"(kw) : "memory");
+        // no "memory" clobber: nothing in a filter kernel reads the
+        // aggregation buffers, and the clobber would make the compiler
+        // reload every operand of the loop after each reduction
+        asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(A.pair + 2 * o), "f"(v), "f"(kw));
     } else {
         atomicAdd(A.num + o, v);
         atomicAdd(A.den + o, kw);
@@ -200,12 +203,15 @@ __device__ __forceinline__ void gather_k(const StepHead& P, const float* __restr
                                          int nsx, int log2n, float* g, int lane)
 {
     constexpr int K2 = K * K;
+    // geometry in registers before the first copy (cp_async4s)
     const int total = P.C * nsx * K2;
+    const long long W = P.W, wh = P.wh;
+    const unsigned g0 = smem_addr(g);
     for (int e = lane; e < total; e += 32) {
         const int sl = e / K2, pq = e - sl * K2;
         const int c = sl >> log2n, n = sl & (nsx - 1);
         const int p = pq / K, q = pq - p * K;
-        cp_async4(g + sl * SS + pq, vid + idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q);
+        cp_async4s(g0 + 4u * (unsigned)(sl * SS + pq), vid + idx[n] + c * wh + p * W + q);
     }
 }
 
@@ -389,12 +395,13 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
 
     // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
     const int total = nsl * K2;
+    const size_t W = (size_t)P.W, wh = (size_t)P.wh;
     for (int e = lane; e < total; e += 32) {
         const int sl = e / K2, pq = e - sl * K2;
         const int c = sl >> log2n, n = sl & (nsx - 1);
         const int p = pq / K, q = pq - p * K;
         const float kw = T.kaiser[pq] * wgt[c];
-        agg_add<PAIR>(A, idx[n] + (size_t)c * P.wh + (size_t)p * P.W + q, kw * ge[sl * SS + pq], kw);
+        agg_add<PAIR>(A, idx[n] + (size_t)c * wh + (size_t)p * W + q, kw * ge[sl * SS + pq], kw);
     }
 }
 
