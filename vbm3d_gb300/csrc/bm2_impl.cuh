@@ -28,7 +28,7 @@ struct PWin {
     int tile;               // float offset of its staged tile
     int res;                // offset of its results in the phase result array
     int chain;              // 0: reference frame, 1: forward, 2: backward
-    float rcp_ww;           // 1 / ww, to split positions into (row, column)
+    int pad;
     unsigned long long seen;  // earlier windows on the same frame (bit i: scanned window i)
 };
 
@@ -48,9 +48,6 @@ __device__ __forceinline__ void unpack_xyt(unsigned v, int rt, int& x, int& y, i
     y = (int)((v >> 13) & 8191u);
     t = (int)(v >> 26) - 32 + rt;
 }
-
-// Row of position j in a window of width ww (exact: j < 2^8, ww <= 15).
-__device__ __forceinline__ int pos_row(int j, float rcp_ww) { return (int)(((float)j + 0.5f) * rcp_ww); }
 
 constexpr unsigned kNone = 0xffffffffu;
 
@@ -274,6 +271,31 @@ __host__ __device__ __forceinline__ int bm2_tile_offset(int w, int tile_sz)
     return (w >> 1) * bm2_pair_stride(tile_sz) + (w & 1) * tile_sz;
 }
 
+// One phase entry: position (dy, cx) of window W with squared-difference
+// sum acc, unless it lies outside the window; an entry seen in an earlier
+// window of the same frame is stored as not a candidate (i == kNone).
+__device__ __forceinline__ void store_entry(const StepHead& P, const Smem& S, const PWin& W, int dy, int cx,
+                                            float acc, float norm, int rx, int ry, int rt)
+{
+    if (dy >= W.wh || cx >= W.ww) return;
+    const int qx = W.x0 + cx, qy = W.y0 + dy;
+    bool seen = false;
+    for (unsigned long long m = W.seen; m; m &= m - 1) {
+        const Win v = S.wins[__ffsll((long long)m) - 1];
+        if (qx >= v.x0 && qx <= v.x1 && qy >= v.y0 && qy <= v.y1) {
+            seen = true;
+            break;
+        }
+    }
+    Pair e{0.f, kNone};
+    if (!seen) {
+        float d = acc / norm;
+        if (qx == rx && qy == ry) d = d - P.dbias;
+        e = Pair{d, pack_xyt(qx, qy, W.t, rt)};
+    }
+    S.res[W.res + dy * W.ww + cx] = e;
+}
+
 // Distances of every position of the phase's nw windows.  Windows are
 // taken in pairs (0, 1), (2, 3), ...; a lane owns one slot (dy, 2cx) of a
 // pair and evaluates positions (dy, 2cx) and (dy, 2cx + 1) of both windows
@@ -282,70 +304,64 @@ __host__ __device__ __forceinline__ int bm2_tile_offset(int w, int tile_sz)
 // each packed f32x2 operation.  An odd last window runs in passes of its
 // own, a lane evaluating positions (dy, 2cx) and (dy, 2cx + 1) of it as the
 // packed pair.  Every distance is the reference's sequential sum over
-// (c, hy, hx).
+// (c, hy, hx).  Only the slot (window, dy, dx) is live across the sums; the
+// windows' fields are read again for the results.
 template <int K, int C>
 __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
                                 int pitch, int plane)
 {
     constexpr int KK = K * K;
     const int npairs = nw >> 1;
-    int pstart[kMaxNb + 1];
-    int total = 0;
-#pragma unroll
-    for (int p = 0; p < kMaxNb; p++) {
-        pstart[p] = total;
-        if (p < npairs) {
-            const PWin& A = S.pw[2 * p];
-            const PWin& B = S.pw[2 * p + 1];
-            total += max(A.wh, B.wh) * ((max(A.ww, B.ww) + 1) >> 1);
-        }
+    // pair `lane` (lanes < npairs): `cols` slot columns (ceil(max ww / 2)),
+    // max wh rows; pend = one past its last slot (inclusive scan)
+    int cols = 1, slots = 0;
+    if (lane < npairs) {
+        const PWin& A = S.pw[2 * lane];
+        const PWin& B = S.pw[2 * lane + 1];
+        cols = (max(A.ww, B.ww) + 1) >> 1;
+        slots = max(A.wh, B.wh) * cols;
     }
-    pstart[kMaxNb] = total;
+    int pend = slots;
+#pragma unroll
+    for (int o = 1; o < kMaxNb; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, pend, o);
+        if (lane >= o) pend += v;
+    }
+    const int total = npairs > 0 ? __shfl_sync(kFull, pend, npairs - 1) : 0;
     const int pair_passes = (total + 31) >> 5;
-    const int lone_slots = (nw & 1) ? S.pw[nw - 1].wh * ((S.pw[nw - 1].ww + 1) >> 1) : 0;
+    int lone_cols = 1, lone_slots = 0;
+    if (nw & 1) {
+        const PWin& L = S.pw[nw - 1];
+        lone_cols = (L.ww + 1) >> 1;
+        lone_slots = L.wh * lone_cols;
+    }
     const int passes = pair_passes + ((lone_slots + 31) >> 5);
     const float nz = P.neg_zero;
+    const float norm = (float)(KK * C);
 
     for (int pass = 0; pass < passes; pass++) {
         const bool pm = pass < pair_passes;  // uniform over the warp
         const int sl = (pm ? pass : pass - pair_passes) * 32 + lane;
-        const float* tA = S.tiles;
-        const float* tB = S.tiles;
-        int rslot[4], qxy[4], win[4];
-        bool valid[4] = {false, false, false, false};
-        {
-            int wa = nw - 1, wb = nw - 1, j = sl, limit = lone_slots;
-            if (pm) {
-                int p = 0;
-#pragma unroll
-                for (int q = 1; q < kMaxNb; q++) p += (q < npairs && sl >= pstart[q]) ? 1 : 0;
-                wa = 2 * p;
-                wb = 2 * p + 1;
-                j = sl - pstart[p];
-                limit = total - pstart[p];
-                limit = p + 1 < npairs ? pstart[p + 1] - pstart[p] : limit;
-            }
-            if (j < limit) {
-                const PWin A = S.pw[wa];
-                const PWin B = S.pw[wb];
-                const int cp = (max(A.ww, B.ww) + 1) >> 1;
-                const int dy = pos_row(j, 1.0f / (float)cp), dx = 2 * (j - dy * cp);
-                tA = S.tiles + A.tile + dy * pitch + dx;
-                tB = S.tiles + B.tile + dy * pitch + dx;
-                // candidates: pairs (A dx, B dx, A dx+1, B dx+1); lone (A dx, A dx+1)
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const bool second = pm ? (q & 1) : false;
-                    const int w = second ? wb : wa;
-                    const PWin& W = second ? B : A;
-                    const int cx = dx + (pm ? (q >> 1) : q);
-                    valid[q] = (pm || q < 2) && dy < W.wh && cx < W.ww;
-                    win[q] = w;
-                    rslot[q] = W.res + dy * W.ww + cx;
-                    qxy[q] = ((W.y0 + dy) << 16) | (W.x0 + cx);
-                }
-            }
+        // the lane's slot: window wa (pairs: and wa + 1), row dy, column dx
+        int wa = nw - 1, j = sl, limit = lone_slots, cp = lone_cols;
+        if (pm) {
+            int p = 0;
+            for (int q = 0; q + 1 < npairs; q++) p += sl >= __shfl_sync(kFull, pend, q) ? 1 : 0;
+            const int e = __shfl_sync(kFull, pend, p), n = __shfl_sync(kFull, slots, p);
+            cp = __shfl_sync(kFull, cols, p);
+            wa = 2 * p;
+            j = sl - (e - n);
+            limit = n;
         }
+        const bool act = j < limit;
+        // row of slot j: (j + 0.5) / cp lies at least 0.5 / cp from an
+        // integer, and the approximate reciprocal (2 ulp) moves it by less
+        // for every j < 2^20, so the truncation is exact
+        const int dy = act ? (int)(((float)j + 0.5f) * __fdividef(1.0f, (float)cp)) : 0;
+        const int dx = act ? 2 * (j - dy * cp) : 0;
+        const int roff = dy * pitch + dx;
+        const float* tA = S.tiles + (act ? S.pw[wa].tile + roff : 0);
+        const float* tB = S.tiles + (act && pm ? S.pw[wa + 1].tile + roff : 0);
         float a0x = 0.f, a0y = 0.f, a1x = 0.f, a1y = 0.f;
         if (pm) {
 #pragma unroll 1
@@ -387,36 +403,19 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
                 }
             }
         }
-        const float acc[4] = {a0x, a0y, a1x, a1y};
-        const float norm = (float)(KK * C);
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (!valid[q]) continue;
-            // pairs: q -> (a0x, a0y, a1x, a1y); lone: q 0, 1 -> (a0x, a0y)
-            const PWin& pwn = S.pw[win[q]];
-            const int qx = qxy[q] & 0xffff, qy = qxy[q] >> 16;
-            // seen: inside an earlier window on the same frame
-            bool seen = false;
-            unsigned long long m = pwn.seen;
-            while (m) {
-                const int wi = __ffsll((long long)m) - 1;
-                m &= m - 1;
-                const Win v = S.wins[wi];
-                if (qx >= v.x0 && qx <= v.x1 && qy >= v.y0 && qy <= v.y1) {
-                    seen = true;
-                    break;
-                }
+        if (act) {
+            // pairs: (A dx, B dx, A dx+1, B dx+1) -> (a0x, a0y, a1x, a1y);
+            // lone: (A dx, A dx+1) -> (a0x, a0y)
+            const PWin A = S.pw[wa];
+            store_entry(P, S, A, dy, dx, a0x, norm, rx, ry, rt);
+            if (pm) {
+                const PWin B = S.pw[wa + 1];
+                store_entry(P, S, B, dy, dx, a0y, norm, rx, ry, rt);
+                store_entry(P, S, A, dy, dx + 1, a1x, norm, rx, ry, rt);
+                store_entry(P, S, B, dy, dx + 1, a1y, norm, rx, ry, rt);
+            } else {
+                store_entry(P, S, A, dy, dx + 1, a0y, norm, rx, ry, rt);
             }
-            Pair e;
-            e.i = kNone;
-            e.d = 0.f;
-            if (!seen) {
-                float d = acc[q] / norm;
-                if (qx == rx && qy == ry) d = d - P.dbias;
-                e.d = d;
-                e.i = pack_xyt(qx, qy, pwn.t, rt);
-            }
-            S.res[rslot[q]] = e;
         }
     }
     __syncwarp();
@@ -485,7 +484,7 @@ __device__ __forceinline__ PWin make_window(const StepHead& P, int t, int cx, in
     w.chain = chain;
     w.tile = 0;
     w.res = 0;
-    w.rcp_ww = 1.0f / (float)w.ww;
+    w.pad = 0;
     w.seen = 0ull;
     return w;
 }
