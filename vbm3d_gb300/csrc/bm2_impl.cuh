@@ -105,18 +105,20 @@ __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) &
 __device__ __forceinline__ int npos(const PWin& w) { return w.ww * w.wh; }
 
 // The m smallest valid entries of res[0..n) (scan order), sorted into
-// out[0..m) by the restatement of the reference's partial_sort on lane 0:
-// the order among equal distances that std::partial_sort leaves.
+// out[0..m) by the restatement of the reference's partial_sort on one
+// thread: the order among equal distances that std::partial_sort leaves.
+__device__ void tie_sort(const Pair* res, int n, int m, Pair* out, Pair* scratch)
+{
+    int k = 0;
+    for (int j = 0; j < n; j++)
+        if (res[j].i != kNone) scratch[k++] = res[j];
+    partial_sort(scratch, m, k);
+    for (int r = 0; r < m; r++) out[r] = scratch[r];
+}
 __device__ void tie_fallback(const Pair* res, int n, int m, int lane, Pair* out, Pair* scratch)
 {
     __syncwarp();
-    if (lane == 0) {
-        int k = 0;
-        for (int j = 0; j < n; j++)
-            if (res[j].i != kNone) scratch[k++] = res[j];
-        partial_sort(scratch, m, k);
-        for (int r = 0; r < m; r++) out[r] = scratch[r];
-    }
+    if (lane == 0) tie_sort(res, n, m, out, scratch);
 }
 
 constexpr unsigned kNoKey = 0xffffffffu;   // no entry: above every key
@@ -259,6 +261,92 @@ __device__ void small_partial_sort(Pair* a, int m, int n, int lane)
         partial_sort(a, m, n);
     }
     __syncwarp();
+}
+
+// select_window for every window of a phase at once (nw <= 32 / G, each
+// window at most 32 positions): window w on the G lanes of group w, up to
+// 32 / G entries per lane, each rank one group minimum of the keys and one
+// group count of the entries holding it.  The picks of the windows of a
+// chain are appended in window order to the chain's frame candidates
+// (S.fc: forward chain first), as the per-window calls append them; nfc_f
+// and nfc_b count them.  Windows with a tie (or a NaN) at a rank go, one
+// at a time, to the partial_sort restatement on their group's first lane.
+template <int G>
+__device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, int lane, int& nfc_f, int& nfc_b)
+{
+    constexpr int E = 32 / G;
+    const int Nb = P.Nb;
+    const int w = lane / G, gl = lane & (G - 1);
+    int n = 0, res = 0;
+    if (w < nw) {
+        const PWin& W = S.pw[w];
+        n = W.ww * W.wh;
+        res = W.res;
+    }
+    unsigned key[E], idx[E];
+    unsigned nv = 0;
+#pragma unroll
+    for (int i = 0; i < E; i++) {
+        const int j = gl + G * i;
+        key[i] = kNoKey;
+        idx[i] = 0;
+        if (j < n) {
+            const Pair e = S.res[res + j];
+            if (e.i != kNone) {
+                key[i] = dist_key(e.d);
+                idx[i] = e.i;
+                nv++;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) nv += __shfl_xor_sync(kFull, nv, o);
+    const int m = min(Nb, (int)nv);  // 0 for the groups past nw
+    // the window's chain (forward: windows 0 .. Nb-1 when the forward
+    // chain is active) and its offset among the chain's candidates
+    const bool fwd = fa && w < Nb;
+    const int c0 = fwd ? 0 : (fa ? Nb : 0);
+    int off = 0, nf = 0, nb = 0;
+#pragma unroll
+    for (int v = 0; v < E; v++) {
+        const int mv = __shfl_sync(kFull, m, v * G);
+        if (fa && v < Nb) nf += mv;
+        else nb += mv;
+        if (v >= c0 && v < w) off += mv;
+    }
+    Pair* out = S.fc + (fwd ? 0 : Nb * Nb) + off;
+    bool tie = false;
+    for (int r = 0; r < Nb; r++) {
+        unsigned gmin = key[0];
+#pragma unroll
+        for (int i = 1; i < E; i++) gmin = min(gmin, key[i]);
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) gmin = min(gmin, (unsigned)__shfl_xor_sync(kFull, gmin, o));
+        unsigned c = 0;
+#pragma unroll
+        for (int i = 0; i < E; i++) c += key[i] == gmin ? 1u : 0u;
+        unsigned cs = c;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) cs += __shfl_xor_sync(kFull, cs, o);
+        if (tie || r >= m) continue;  // uniform over the group
+        if (gmin == kNanKey || cs != 1u) {
+            tie = true;
+            continue;
+        }
+#pragma unroll
+        for (int i = 0; i < E; i++)
+            if (key[i] == gmin) {
+                out[r] = Pair{key_dist(gmin), idx[i]};
+                key[i] = kNoKey;
+            }
+    }
+    __syncwarp();
+    for (unsigned tb = __ballot_sync(kFull, gl == 0 && tie); tb; tb &= tb - 1) {
+        if (lane == __ffs(tb) - 1) tie_sort(S.res + res, n, m, out, S.scr);
+        __syncwarp();
+    }
+    nfc_f = nf;
+    nfc_b = nb;
 }
 
 // Float offset of the staged tile of window w of a phase whose tiles hold
@@ -619,13 +707,23 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
         phase_distances<K, C>(P, S, nw, lane, rx, ry, rt, pitch, plane);
 
         // per chain: top-Nb of each window, then of their union
-        int w0 = 0;
+        int nfc2[2] = {0, 0};
+        if (nw <= 4 && P.Npr * P.Npr <= 32) {
+            if (nw <= 2) select_phase<16>(P, S, nw, fa, lane, nfc2[0], nfc2[1]);
+            else select_phase<8>(P, S, nw, fa, lane, nfc2[0], nfc2[1]);
+        } else {
+            int w0 = 0;
+            for (int chain = 1; chain <= 2; chain++) {
+                if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
+                for (int m = 0; m < Nb; m++)
+                    select_window(P, S, S.pw[w0 + m], lane, S.fc + (chain - 1) * Nb * Nb, nfc2[chain - 1], S.scr);
+                w0 += Nb;
+            }
+        }
         for (int chain = 1; chain <= 2; chain++) {
             if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
             Pair* fc = S.fc + (chain - 1) * Nb * Nb;
-            int nfc = 0;
-            for (int m = 0; m < Nb; m++) select_window(P, S, S.pw[w0 + m], lane, fc, nfc, S.scr);
-            w0 += Nb;
+            const int nfc = nfc2[chain - 1];
             const int m2 = min(Nb, nfc);
             small_partial_sort(fc, m2, nfc, lane);
             Pair* dst = chain == 1 ? bestf + nbf : bestb + nbb;
