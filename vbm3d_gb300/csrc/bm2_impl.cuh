@@ -88,7 +88,7 @@ __device__ __forceinline__ void sq_acc2(float& ax, float& ay, float rx, float ry
 
 struct Smem {
     Pair* scr;     // tie fallback scratch
-    float2* refp;  // C*k*k duplicated reference pixels
+    float2* refp;  // duplicated reference pixels, rows of bm2_ref_row(k) (padded to even)
     float* tiles;  // staged windows of the phase
     Win* wins;     // every window scanned so far
     PWin* pw;      // windows of the current phase
@@ -100,6 +100,10 @@ struct Smem {
 };
 
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Row length (float2 entries) of the staged reference patch: k rounded up
+// to even, so that each 16-byte load brings two duplicated pixels.
+__host__ __device__ __forceinline__ int bm2_ref_row(int k) { return (k + 1) & ~1; }
 
 // Number of positions of a window.
 __device__ __forceinline__ int npos(const PWin& w) { return w.ww * w.wh; }
@@ -398,7 +402,7 @@ template <int K, int C>
 __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
                                 int pitch, int plane)
 {
-    constexpr int KK = K * K;
+    constexpr int KK = K * K, KR = (K + 1) & ~1;  // KR: bm2_ref_row(K)
     const int npairs = nw >> 1;
     // pair `lane` (lanes < npairs): `cols` slot columns (ceil(max ww / 2)),
     // max wh rows; pend = one past its last slot (inclusive scan)
@@ -456,7 +460,7 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
             for (int c = 0; c < C; c++) {
                 const float* pa = tA + c * plane;
                 const float* pb = tB + c * plane;
-                const float2* rr = S.refp + c * KK;
+                const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
 #pragma unroll 1
                 for (int hy = 0; hy < K; hy++) {
                     float va[K + 1], vb[K + 1];
@@ -465,11 +469,16 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
                         va[x] = pa[hy * pitch + x];
                         vb[x] = pb[hy * pitch + x];
                     }
+                    // terms hx, hx + 1 of both accumulators, in order
 #pragma unroll
-                    for (int hx = 0; hx < K; hx++) {
-                        const float2 r2 = rr[hy * K + hx];
-                        sq_acc2(a0x, a0y, r2.x, r2.y, va[hx], vb[hx], nz);
-                        sq_acc2(a1x, a1y, r2.x, r2.y, va[hx + 1], vb[hx + 1], nz);
+                    for (int hx = 0; hx < K; hx += 2) {
+                        const float4 r4 = rr[(hy * KR + hx) >> 1];
+                        sq_acc2(a0x, a0y, r4.x, r4.y, va[hx], vb[hx], nz);
+                        sq_acc2(a1x, a1y, r4.x, r4.y, va[hx + 1], vb[hx + 1], nz);
+                        if (hx + 1 < K) {
+                            sq_acc2(a0x, a0y, r4.z, r4.w, va[hx + 1], vb[hx + 1], nz);
+                            sq_acc2(a1x, a1y, r4.z, r4.w, va[hx + 2], vb[hx + 2], nz);
+                        }
                     }
                 }
             }
@@ -477,16 +486,17 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
                 const float* pa = tA + c * plane;
-                const float2* rr = S.refp + c * KK;
+                const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
 #pragma unroll 1
                 for (int hy = 0; hy < K; hy++) {
                     float va[K + 1];
 #pragma unroll
                     for (int x = 0; x <= K; x++) va[x] = pa[hy * pitch + x];
 #pragma unroll
-                    for (int hx = 0; hx < K; hx++) {
-                        const float2 r2 = rr[hy * K + hx];
-                        sq_acc2(a0x, a0y, r2.x, r2.y, va[hx], va[hx + 1], nz);
+                    for (int hx = 0; hx < K; hx += 2) {
+                        const float4 r4 = rr[(hy * KR + hx) >> 1];
+                        sq_acc2(a0x, a0y, r4.x, r4.y, va[hx], va[hx + 1], nz);
+                        if (hx + 1 < K) sq_acc2(a0x, a0y, r4.z, r4.w, va[hx + 1], va[hx + 2], nz);
                     }
                 }
             }
@@ -591,7 +601,7 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
     Smem S;
     size_t off = 0;
     S.refp = reinterpret_cast<float2*>(ws + off);
-    off = align16(off + sizeof(float2) * C * KK);
+    off = align16(off + sizeof(float2) * C * K * bm2_ref_row(K));
     S.tiles = reinterpret_cast<float*>(ws + off);
     off = align16(off + sizeof(float) * L.tile_floats);
     S.res = reinterpret_cast<Pair*>(ws + off);
@@ -615,7 +625,7 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
     for (int e = lane; e < C * KK; e += 32) {
         const int c = e / KK, pq = e - c * KK, py = pq / K, px = pq - py * K;
         const float v = __ldg(vid + (size_t)rt * P.whc + (size_t)c * P.wh + (size_t)(ry + py) * P.W + rx + px);
-        S.refp[e] = make_float2(v, v);
+        S.refp[(c * K + py) * bm2_ref_row(K) + px] = make_float2(v, v);
     }
     if (lane == 0) {
         S.cnt[2] = 0;  // windows scanned
@@ -792,7 +802,7 @@ inline Layout bm2_layout(const StepHead& P)
     L.res_cap = max(max(P.Ns * P.Ns, 2 * P.Nb * P.Npr * P.Npr), P.Nb * (1 + 2 * P.Nf));
     L.scr_cap = max(P.Ns * P.Ns, P.Npr * P.Npr);
     // the same sequence of 16-byte aligned regions as the kernel
-    size_t off = align16(sizeof(float2) * P.C * P.k * P.k);
+    size_t off = align16(sizeof(float2) * P.C * P.k * bm2_ref_row(P.k));
     off = align16(off + sizeof(float) * L.tile_floats);
     off = align16(off + sizeof(Pair) * L.res_cap);
     off = align16(off + sizeof(Pair) * L.scr_cap);
