@@ -253,9 +253,9 @@ def fp32_peak(dev, clocks):
 # DRAM bytes (read + write) per reference patch of the batched step-2 block
 # matching of the RGB k = 7 clips: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of batch_bm_kernel<2, 7, 3> on the full batch
-# (python -m vbm3d_gb300.profile_case --batch 64): 1.48 GB + 0.439 GB for
+# (python -m vbm3d_gb300.profile_case --batch 64): 1.449 GB + 0.437 GB for
 # 12 308 991 reference patches.
-BM2_DRAM_BYTES_PER_REF = 156.0
+BM2_DRAM_BYTES_PER_REF = 153.0
 
 
 def timed(stream, fn, steps):

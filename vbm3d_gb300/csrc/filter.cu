@@ -182,7 +182,7 @@ filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const
     if (r >= P.nrefs) return;
 
     const int k = P.k, k2 = k * k, C = P.C, kt = P.kt;
-    const int ss = k2 + 1;  // slice stride
+    const int ss = k2 | 1;  // slice stride, odd: a lane per slice reads on distinct banks
     float* base = fsm + (size_t)wid * warp_floats;
     int* traj = reinterpret_cast<int*>(base);                // [n][ht]: top-left offset in channel 0
     float* gA = base + kMaxN * kMaxKt;                      // noisy group (step 1: the group)

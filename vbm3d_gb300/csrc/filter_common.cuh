@@ -364,7 +364,8 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
                                            const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
                                            const AggTarget& A)
 {
-    constexpr int K2 = K * K, SS = K2 + 1;
+    // odd slice stride: a lane per slice reads on distinct banks
+    constexpr int K2 = K * K, SS = K2 | 1;
     const int C = P.C;
     unsigned* idx = reinterpret_cast<unsigned*>(base);
     float* gA = base + kMaxN;               // noisy group

@@ -203,7 +203,7 @@ linear_kernel(const StepParams P, const float* __restrict__ src, const float* __
               const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx, float* __restrict__ out,
               int warp_floats)
 {
-    constexpr int K2 = K * K, SS = K2 + 1;
+    constexpr int K2 = K * K, SS = K2 | 1;  // odd: a lane per slice reads on distinct banks
     extern __shared__ __align__(16) float fsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long r = (long long)blockIdx.x * (blockDim.x >> 5) + wid;
