@@ -318,6 +318,39 @@ int vbm3d_gpu_tvl1_pairs(const float *I0, const float *I1, unsigned npairs, unsi
 int vbm3d_gpu_tvl1_video(const float *video, unsigned width, unsigned height, unsigned frames,
                          const vbm3d_tvl1_params *params, float *fflow, float *bflow, void *stream);
 
+/* Multiscaler DCT pyramid: the pre- and post-processing of the reference's
+ * multiscale denoising (src/utils/VBM3Ddenoising_multiscale.sh), which
+ * decomposes every frame into DCT levels, denoises each level with VBM3D at
+ * sigma / 2^level and recomposes the frame.  Replace the `decompose`,
+ * `recompose` and `merge_coarse` programs with the DCT type (-t 0;
+ * multiscaler/decompose.cpp, recompose.cpp, merge_coarse.cpp over
+ * dct_inplace / idct_inplace, multiscaler/multiscaler.cpp:21-100).  Images
+ * are `planes` planar float planes (frames x channels) of height x width
+ * rows, device memory; level i is the previous level halved by integer
+ * division (level 0 is the full size).  The transforms are FFTW's REDFT10 /
+ * REDFT01 in float, so results match the reference to float rounding.
+ * Asynchronous on `stream`.
+ *
+ * decompose: out[0 .. levels) receive the levels ([planes][h_i][w_i]). */
+int vbm3d_gpu_ms_decompose(const float *in, unsigned width, unsigned height, unsigned planes,
+                           unsigned levels, float *const *out, void *stream);
+
+/* recompose: level_in[0 .. levels) hold the (denoised) levels, out the
+ * full-size image: level 0's DCT with the block of rows < h_i * factor and
+ * columns < w_i * factor (float product, as the reference's loop bound) of
+ * every coarser level's DCT written over it, then the inverse DCT.
+ * VBM3D_ERR_INVALID_ARGUMENT for factor > 1 (the reference would read past
+ * the level). */
+int vbm3d_gpu_ms_recompose(const float *const *level_in, unsigned width, unsigned height,
+                           unsigned planes, unsigned levels, float factor, float *out, void *stream);
+
+/* merge_coarse: the fine image's DCT with the coarse image's low-frequency
+ * block (rows < cheight * factor, columns < cwidth * factor) written over
+ * it, then the inverse DCT, into out (width x height planes). */
+int vbm3d_gpu_ms_merge_coarse(const float *fine, const float *coarse, unsigned width,
+                              unsigned height, unsigned cwidth, unsigned cheight, unsigned planes,
+                              float factor, float *out, void *stream);
+
 /* Measurement helper with no reference counterpart: runs the block
  * matching of vbm3d_gpu_similar_patches and returns in *count the total
  * number of patch distances it evaluated (calls of the reference's

@@ -11,6 +11,9 @@
 #   oracle/_ref/libtvl1_ref.so   the reference's TV-L1 library
 #       (tvl1flow/tvl1flow_lib.c and the files it includes), single thread,
 #       no FP contraction: the pin of the TV-L1 restatement
+#   oracle/_ref/libms_ref.so   the reference's multiscaler programs
+#       (multiscaler/{multiscaler,decompose,recompose,merge_coarse}.cpp):
+#       the pin of the multiscaler restatement
 # FFTW3f is not installed: oracle/fftw_shim supplies REDFT10/REDFT01.
 set -e
 REF=${1:-/root/reference}
@@ -36,4 +39,18 @@ build libvbm3d_ref_exact.so -O2 -ffp-contract=off -fno-fast-math
 build libvbm3d_ref_fast.so -O3 -ffast-math -fomit-frame-pointer
 gcc -std=c99 -w -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -I"$REF/tvl1flow" \
     "$HERE/ref_harness/tvl1_ref_harness.c" -lm -o "$OUT/libtvl1_ref.so"
+# the multiscaler programs, each main renamed, over the FFTW stand-in and
+# an in-memory image table (ms_ref_harness.cpp) in place of iio
+MS="$REF/multiscaler"
+tmp=$(mktemp -d)
+MSFLAGS="-std=c++11 -w -O2 -ffp-contract=off -fno-fast-math -fPIC -I$HERE/fftw_shim -I$MS"
+g++ $MSFLAGS -c "$MS/multiscaler.cpp" -o "$tmp/multiscaler.o" &
+g++ $MSFLAGS -Dmain=ms_decompose_main -c "$MS/decompose.cpp" -o "$tmp/decompose.o" &
+g++ $MSFLAGS -Dmain=ms_recompose_main -c "$MS/recompose.cpp" -o "$tmp/recompose.o" &
+g++ $MSFLAGS -Dmain=ms_merge_coarse_main -c "$MS/merge_coarse.cpp" -o "$tmp/merge_coarse.o" &
+g++ $MSFLAGS -c "$HERE/ref_harness/ms_ref_harness.cpp" -o "$tmp/ms_ref_harness.o" &
+gcc -std=c99 -O2 -ffp-contract=off -fno-fast-math -fPIC -I"$HERE/fftw_shim" -c "$HERE/fftw_shim/fftw_shim.c" -o "$tmp/fftw_shim.o" &
+wait
+g++ -shared -o "$OUT/libms_ref.so" "$tmp"/*.o -lm
+rm -rf "$tmp"
 echo "built $OUT"

@@ -5,8 +5,9 @@
  * against this header and fftw_shim.c because libfftw3f is not installed.
  * Only the r2r surface the reference calls is declared
  * (src/Utilities/Utilities.cpp:346-398, src/vbm3d.cpp:1242-1303,
- * :1693-1712, :1882-1955).  The enumerator values are this shim's own; the
- * reference only passes them back to the shim.
+ * :1693-1712, :1882-1955, multiscaler/multiscaler.cpp:21-100).  The
+ * enumerator values are this shim's own; the reference only passes them
+ * back to the shim.
  */
 #ifndef ORACLE_FFTW3_SHIM_H
 #define ORACLE_FFTW3_SHIM_H
@@ -35,6 +36,7 @@ fftwf_plan fftwf_plan_many_r2r(int rank, const int *n, int howmany,
                                float *out, const int *onembed, int ostride, int odist,
                                const fftwf_r2r_kind *kind, unsigned flags);
 void fftwf_execute_r2r(const fftwf_plan p, float *in, float *out);
+void fftwf_execute(const fftwf_plan p);
 void fftwf_destroy_plan(fftwf_plan p);
 void fftwf_cleanup(void);
 

@@ -12,22 +12,23 @@
  * multi-dimensional r2r definition.  Real FFTW computes the same values in
  * float with its own rounding; the difference is a few float ulps.
  * The oracle restatement (vbm3d_oracle.c) calls the same routines, so both
- * oracles see identical transform values.
+ * oracles see identical transform values.  The multiscaler's whole-frame
+ * plans (multiscaler/multiscaler.cpp:21-100) run through fftwf_execute on
+ * the plan's own buffers; sizes are unlimited (O(n^2) per line).
  */
 #include "fftw3.h"
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
-#define SHIM_MAXN 64
-
 struct oracle_fftwf_plan_s {
     int rank;
     int n[2];
     int howmany;
     int istride, idist, ostride, odist;
+    float *in, *out;
     fftwf_r2r_kind kind[2];
-    double cosv[2][SHIM_MAXN * SHIM_MAXN]; /* cosv[axis][k*n + j] */
+    double *cosv[2]; /* cosv[axis][k*n + j] */
 };
 
 /* calloc: dct_2d_inv transforms its whole buffer, of which only the
@@ -50,8 +51,8 @@ fftwf_plan fftwf_plan_many_r2r(int rank, const int *n, int howmany,
                                float *out, const int *onembed, int ostride, int odist,
                                const fftwf_r2r_kind *kind, unsigned flags)
 {
-    (void)in; (void)out; (void)inembed; (void)onembed; (void)flags;
-    if (rank < 1 || rank > 2 || n[0] > SHIM_MAXN || (rank == 2 && n[1] > SHIM_MAXN)) return NULL;
+    (void)inembed; (void)onembed; (void)flags;
+    if (rank < 1 || rank > 2 || n[0] < 1 || (rank == 2 && n[1] < 1)) return NULL;
     struct oracle_fftwf_plan_s *p = (struct oracle_fftwf_plan_s *)calloc(1, sizeof(*p));
     p->rank = rank;
     p->n[0] = n[0];
@@ -59,19 +60,30 @@ fftwf_plan fftwf_plan_many_r2r(int rank, const int *n, int howmany,
     p->howmany = howmany;
     p->istride = istride; p->idist = idist;
     p->ostride = ostride; p->odist = odist;
+    p->in = in; p->out = out;
     p->kind[0] = kind[0];
     p->kind[1] = rank == 2 ? kind[1] : kind[0];
+    p->cosv[0] = (double *)malloc(sizeof(double) * (size_t)p->n[0] * p->n[0]);
     fill_cos(p->cosv[0], p->n[0], p->kind[0]);
-    if (rank == 2) fill_cos(p->cosv[1], p->n[1], p->kind[1]);
+    if (rank == 2) {
+        p->cosv[1] = (double *)malloc(sizeof(double) * (size_t)p->n[1] * p->n[1]);
+        fill_cos(p->cosv[1], p->n[1], p->kind[1]);
+    }
     return p;
 }
 
-void fftwf_destroy_plan(fftwf_plan p) { free(p); }
-
-/* One 1D transform of length n on a strided double vector, in place. */
-static void r2r_1d(double *v, int n, int stride, fftwf_r2r_kind kind, const double *c)
+void fftwf_destroy_plan(fftwf_plan p)
 {
-    double tmp[SHIM_MAXN];
+    if (!p) return;
+    free(p->cosv[0]);
+    free(p->cosv[1]);
+    free(p);
+}
+
+/* One 1D transform of length n on a strided double vector, in place
+ * (tmp: n doubles of scratch). */
+static void r2r_1d(double *v, int n, int stride, fftwf_r2r_kind kind, const double *c, double *tmp)
+{
     for (int k = 0; k < n; k++) {
         double s;
         if (kind == FFTW_REDFT10) {
@@ -90,18 +102,23 @@ static void r2r_1d(double *v, int n, int stride, fftwf_r2r_kind kind, const doub
 void fftwf_execute_r2r(const fftwf_plan p, float *in, float *out)
 {
     const int n0 = p->n[0], n1 = p->n[1];
-    const int sz = n0 * n1;
-    double blk[SHIM_MAXN * SHIM_MAXN];
+    const size_t sz = (size_t)n0 * n1;
+    double *blk = (double *)malloc(sizeof(double) * sz);
+    double *tmp = (double *)malloc(sizeof(double) * (size_t)(n0 > n1 ? n0 : n1));
     for (int h = 0; h < p->howmany; h++) {
         const float *src = in + (size_t)h * p->idist;
         float *dst = out + (size_t)h * p->odist;
-        for (int i = 0; i < sz; i++) blk[i] = (double)src[(size_t)i * p->istride];
+        for (size_t i = 0; i < sz; i++) blk[i] = (double)src[i * p->istride];
         if (p->rank == 1) {
-            r2r_1d(blk, n0, 1, p->kind[0], p->cosv[0]);
+            r2r_1d(blk, n0, 1, p->kind[0], p->cosv[0], tmp);
         } else {
-            for (int r = 0; r < n0; r++) r2r_1d(blk + r * n1, n1, 1, p->kind[1], p->cosv[1]);
-            for (int c = 0; c < n1; c++) r2r_1d(blk + c, n0, n1, p->kind[0], p->cosv[0]);
+            for (int r = 0; r < n0; r++) r2r_1d(blk + (size_t)r * n1, n1, 1, p->kind[1], p->cosv[1], tmp);
+            for (int c = 0; c < n1; c++) r2r_1d(blk + c, n0, n1, p->kind[0], p->cosv[0], tmp);
         }
-        for (int i = 0; i < sz; i++) dst[(size_t)i * p->ostride] = (float)blk[i];
+        for (size_t i = 0; i < sz; i++) dst[i * p->ostride] = (float)blk[i];
     }
+    free(blk);
+    free(tmp);
 }
+
+void fftwf_execute(const fftwf_plan p) { fftwf_execute_r2r(p, p->in, p->out); }

@@ -76,6 +76,10 @@ def load(path=LIB_PATH):
     L.vbm3d_tvl1_scales.argtypes = [C.c_uint, C.c_uint, T, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.vbm3d_gpu_tvl1_pairs.argtypes = [vp, vp, C.c_uint, C.c_uint, C.c_uint, T, vp, C.POINTER(C.c_int), vp]
     L.vbm3d_gpu_tvl1_video.argtypes = [vp, C.c_uint, C.c_uint, C.c_uint, T, vp, vp, vp]
+    L.vbm3d_gpu_ms_decompose.argtypes = [vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.POINTER(vp), vp]
+    L.vbm3d_gpu_ms_recompose.argtypes = [C.POINTER(vp), C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_float, vp, vp]
+    L.vbm3d_gpu_ms_merge_coarse.argtypes = [vp, vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_float,
+                                            vp, vp]
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -278,6 +282,94 @@ def tvl1_video(video, params=None, stream=None):
     bf = torch.empty_like(ff)
     _check(load().vbm3d_gpu_tvl1_video(_ptr(video), w, h, f, C.byref(params), _ptr(ff), _ptr(bf), _stream(stream)))
     return ff, bf
+
+
+def _planes(t, name):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()
+            and t.dim() >= 2):
+        raise TypeError("%s must be a contiguous float32 CUDA tensor [..., H, W]" % name)
+    h, w = t.shape[-2:]
+    return t.numel() // max(h * w, 1), h, w
+
+
+def ms_level_shapes(shape, levels):
+    """Shapes of the DCT pyramid levels of an image stack [..., H, W]:
+    H and W halved by integer division per level."""
+    lead, (h, w) = tuple(shape[:-2]), tuple(shape[-2:])
+    out = []
+    for _ in range(levels):
+        out.append(lead + (h, w))
+        h, w = h // 2, w // 2
+    return out
+
+
+def ms_decompose(x, levels, stream=None):
+    """The multiscaler's DCT pyramid (`decompose ... -t 0`) of a CUDA float32
+    image stack [..., H, W] (every leading index one plane): a list of
+    `levels` stacks, level i halved i times."""
+    import torch
+    p, h, w = _planes(x, "x")
+    outs = [torch.empty(sh, dtype=torch.float32, device=x.device) for sh in ms_level_shapes(x.shape, levels)]
+    ptrs = (C.c_void_p * levels)(*[o.data_ptr() for o in outs])
+    _check(load().vbm3d_gpu_ms_decompose(_ptr(x), w, h, p, levels, ptrs, _stream(stream)))
+    return outs
+
+
+def ms_recompose(levels_in, factor=0.8, stream=None):
+    """`recompose ... -t 0 -c factor`: one stack [..., H, W] from the levels
+    of ms_decompose (possibly denoised)."""
+    import torch
+    p, h, w = _planes(levels_in[0], "levels_in[0]")
+    shapes = ms_level_shapes(levels_in[0].shape, len(levels_in))
+    for i, (lv, sh) in enumerate(zip(levels_in, shapes)):
+        _planes(lv, "levels_in[%d]" % i)
+        if tuple(lv.shape) != sh:
+            raise ValueError("level %d has shape %s, expected %s" % (i, tuple(lv.shape), sh))
+    out = torch.empty_like(levels_in[0])
+    ptrs = (C.c_void_p * len(levels_in))(*[lv.data_ptr() for lv in levels_in])
+    _check(load().vbm3d_gpu_ms_recompose(ptrs, w, h, p, len(levels_in), C.c_float(factor), _ptr(out),
+                                         _stream(stream)))
+    return out
+
+
+def ms_merge_coarse(fine, coarse, factor=0.8, stream=None):
+    """`merge_coarse fine coarse out -c factor` on CUDA float32 stacks
+    [..., H, W] and [..., h, w] with the same leading shape."""
+    import torch
+    p, h, w = _planes(fine, "fine")
+    pc, ch, cw = _planes(coarse, "coarse")
+    if pc != p:
+        raise ValueError("fine and coarse hold different numbers of planes")
+    out = torch.empty_like(fine)
+    _check(load().vbm3d_gpu_ms_merge_coarse(_ptr(fine), _ptr(coarse), w, h, cw, ch, p, C.c_float(factor),
+                                            _ptr(out), _stream(stream)))
+    return out
+
+
+def ms_level_sigma(sigma, level):
+    """The noise level the multiscale script denoises a level with:
+    sigma / 2^level truncated to two decimals (`bc` with scale=2,
+    src/utils/VBM3Ddenoising_multiscale.sh:50)."""
+    from decimal import Decimal, ROUND_DOWN
+    q = Decimal(repr(float(sigma))) / (Decimal(2) ** level)
+    return float(q.quantize(Decimal("0.01"), rounding=ROUND_DOWN))
+
+
+def multiscale_denoise(noisy, sigma, levels=3, factor=0.7, color_space=True, stream=None):
+    """The multiscale denoising of src/utils/VBM3Ddenoising_multiscale.sh on
+    the GPU: every frame of `noisy` (CUDA float32 [F, C, H, W]) decomposed
+    into `levels` DCT levels, each level's clip denoised by VBM3D with the
+    reference's default parameters at ms_level_sigma(sigma, level), and the
+    denoised levels recomposed with `factor` (the script's recomposition
+    ratio, 0.7).  Returns (denoised, denoised levels)."""
+    _video(noisy, "noisy")
+    lv = ms_decompose(noisy, levels, stream=stream)
+    den = []
+    for i, x in enumerate(lv):
+        _, d = run(x.contiguous(), ms_level_sigma(sigma, i), color_space=color_space, stream=stream)
+        den.append(d)
+    return ms_recompose(den, factor, stream=stream), den
 
 
 class Batch:

@@ -1,0 +1,462 @@
+// The multiscaler's DCT pyramid on the GPU (multiscaler/multiscaler.cpp:21-100,
+// decompose.cpp / recompose.cpp type 0, merge_coarse.cpp): the pre- and
+// post-processing of the reference's multiscale denoising script
+// (src/utils/VBM3Ddenoising_multiscale.sh), which splits each frame into
+// DCT levels, denoises every level with VBM3D and merges the levels back.
+//
+// Every transform is FFTW's unnormalised REDFT10 (DCT-II) or REDFT01
+// (DCT-III) of a whole frame, per channel.  Here a 2D transform of P planes
+// of R x W floats is two dense products with cosine matrices: along the
+// rows, one (P*R) x W by W x W product; along the columns, P products of
+// R x R by R x W.  The products run on a batched single-precision tiled
+// kernel (128 x 128 tiles, 8 x 8 outputs per thread, two shared-memory
+// stages, explicit FMA), the cosine matrices are generated on the device in
+// double and rounded to float.  The reference computes the same transforms
+// with FFTW in float; the results agree to float rounding (a few 1e-6 of the
+// data's range), not bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "common.cuh"
+#include "../../include/vbm3d_gb300.h"
+
+namespace vbm3d {
+void set_last_error(int status, const char* msg);
+}
+
+namespace vbm3d {
+namespace ms {
+namespace {
+
+int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int status, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    set_last_error(status, buf);
+    return status;
+}
+
+#define MCK(call)                                                                                              \
+    do {                                                                                                       \
+        cudaError_t e_ = (call);                                                                               \
+        if (e_ != cudaSuccess)                                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? VBM3D_ERR_OUT_OF_MEMORY : VBM3D_ERR_CUDA, "%s: %s", \
+                        #call, cudaGetErrorString(e_));                                                        \
+    } while (0)
+
+// ------------------------------------------------------------ kernels ---
+
+// n x n cosine matrix, row k = output index, column j = input index:
+// REDFT10: 2 cos(pi (j + 1/2) k / n); REDFT01: 1 for j = 0, else
+// 2 cos(pi j (k + 1/2) / n) (FFTW's documented definitions).
+__global__ void cosine_matrix_kernel(float* __restrict__ M, int n, int inverse)
+{
+    const long long total = (long long)n * n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / n), j = (int)(e - (long long)k * n);
+        const double pi = 3.14159265358979323846;
+        double v;
+        if (!inverse) v = 2.0 * cos(pi * (j + 0.5) * k / n);
+        else v = j == 0 ? 1.0 : 2.0 * cos(pi * j * (k + 0.5) / n);
+        M[e] = (float)v;
+    }
+}
+
+struct Gemm {
+    const float* A;  // M x K, row stride lda, batch stride sA
+    const float* B;  // K x N (row stride ldb), or N x K when BT
+    float* C;        // M x N, row stride ldc
+    long long sA, sB, sC;
+    int lda, ldb, ldc;
+    int M, N, K;
+    float div;  // divides every result when != 1
+};
+
+constexpr int BM = 128, BN = 128, BK = 8, kThreads = 256;
+
+// C[b] = A[b] op(B[b]) (op(B) = B^T when BT) in float with FMA, one
+// 128 x 128 tile per block; each thread owns rows {4ty..4ty+3, 64+4ty..}
+// and columns {4tx..4tx+3, 64+4tx..} of the tile.  The next K slice is
+// loaded into registers while the current one is multiplied from shared
+// memory (two stages, one barrier per slice).
+template <bool BT>
+__global__ void __launch_bounds__(kThreads) gemm_kernel(const Gemm g)
+{
+    __shared__ __align__(16) float As[2][BK][BM];
+    __shared__ __align__(16) float Bs[2][BK][BN];
+    const long long b = blockIdx.z;
+    const float* __restrict__ A = g.A + b * g.sA;
+    const float* __restrict__ B = g.B + b * g.sB;
+    float* __restrict__ C = g.C + b * g.sC;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int t = threadIdx.x;
+    // loaders: A (and B^T) rows t / 2, four K columns from (t & 1) * 4;
+    // B: K row t / 32, four N columns from (t & 31) * 4
+    const int lr = t >> 1, lk = (t & 1) * 4;
+    const int bk = t >> 5, bn = (t & 31) * 4;
+    float ra[4], rb[4];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int m = m0 + lr, k = k0 + lk + i;
+            ra[i] = (m < g.M && k < g.K) ? A[(long long)m * g.lda + k] : 0.f;
+        }
+        if (BT) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int n = n0 + lr, k = k0 + lk + i;
+                rb[i] = (n < g.N && k < g.K) ? B[(long long)n * g.ldb + k] : 0.f;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int k = k0 + bk, n = n0 + bn + i;
+                rb[i] = (k < g.K && n < g.N) ? B[(long long)k * g.ldb + n] : 0.f;
+            }
+        }
+    };
+    auto store = [&](int s) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) As[s][lk + i][lr] = ra[i];
+        if (BT) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) Bs[s][lk + i][lr] = rb[i];
+        } else {
+            *reinterpret_cast<float4*>(&Bs[s][bk][bn]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+        }
+    };
+    const int tx = t & 15, ty = t >> 4;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+
+    load(0);
+    store(0);
+    __syncthreads();
+    int s = 0;
+    for (int k0 = 0; k0 < g.K; k0 += BK) {
+        const bool more = k0 + BK < g.K;
+        if (more) load(k0 + BK);
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[s][kk][4 * ty]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[s][kk][64 + 4 * ty]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[s][kk][4 * tx]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[s][kk][64 + 4 * tx]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float c[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(a[i], c[j], acc[i][j]);
+        }
+        if (more) {
+            store(s ^ 1);
+            __syncthreads();
+            s ^= 1;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int m = m0 + (i < 4 ? 4 * ty + i : 64 + 4 * ty + i - 4);
+        if (m >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int n = n0 + (j < 4 ? 4 * tx + j : 64 + 4 * tx + j - 4);
+            if (n < g.N) C[(long long)m * g.ldc + n] = g.div != 1.f ? acc[i][j] / g.div : acc[i][j];
+        }
+    }
+}
+
+// dst[p][r][c] = src[p][r][c] for r < bh, c < bw (row strides ldd, lds;
+// plane strides sd, ss).
+__global__ void copy_block_kernel(float* __restrict__ dst, long long sd, int ldd, const float* __restrict__ src,
+                                  long long ss, int lds, int bh, int bw)
+{
+    const long long p = blockIdx.y;
+    const long long total = (long long)bh * bw;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / bw), c = (int)(e - (long long)r * bw);
+        dst[p * sd + (long long)r * ldd + c] = src[p * ss + (long long)r * lds + c];
+    }
+}
+
+// ---------------------------------------------------------------- host ---
+
+int gemm(bool bt, const Gemm& g, int batch, cudaStream_t s)
+{
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0 || batch <= 0) return VBM3D_OK;
+    const dim3 grid((unsigned)((g.N + BN - 1) / BN), (unsigned)((g.M + BM - 1) / BM), (unsigned)batch);
+    if (grid.y > 65535u || grid.z > 65535u) return fail(VBM3D_ERR_UNSUPPORTED, "matrix product too large");
+    if (bt) gemm_kernel<true><<<grid, kThreads, 0, s>>>(g);
+    else gemm_kernel<false><<<grid, kThreads, 0, s>>>(g);
+    MCK(cudaGetLastError());
+    return VBM3D_OK;
+}
+
+int cosine_matrix(float* M, int n, bool inverse, cudaStream_t s)
+{
+    const long long total = (long long)n * n;
+    const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 4096);
+    cosine_matrix_kernel<<<blocks, 256, 0, s>>>(M, n, inverse ? 1 : 0);
+    MCK(cudaGetLastError());
+    return VBM3D_OK;
+}
+
+// Scratch of one call: two plane stacks of the largest size and the
+// cosine matrices of every size the call uses.
+struct Scratch {
+    float* base = nullptr;
+    cudaStream_t s = nullptr;
+    ~Scratch()
+    {
+        if (base) cudaFreeAsync(base, s);
+    }
+};
+
+// 2D DCT (dct_inplace) of P planes of R x W (contiguous) into Y, each value
+// divided by float(4 R W); T: P R W scratch; Dw, Dr: REDFT10 matrices.
+int dct2d(const float* X, int P, int R, int W, const float* Dw, const float* Dr, float* T, float* Y, cudaStream_t s)
+{
+    Gemm g{};
+    // along the rows: T[(p r)][k] = sum_j X[(p r)][j] Dw[k][j]
+    g.A = X; g.lda = W; g.sA = 0;
+    g.B = Dw; g.ldb = W; g.sB = 0;
+    g.C = T; g.ldc = W; g.sC = 0;
+    g.M = P * R; g.N = W; g.K = W; g.div = 1.f;
+    int rc = gemm(true, g, 1, s);
+    if (rc) return rc;
+    // along the columns: Y[p][k][c] = sum_r Dr[k][r] T[p][r][c] / (4 R W)
+    g.A = Dr; g.lda = R; g.sA = 0;
+    g.B = T; g.ldb = W; g.sB = (long long)R * W;
+    g.C = Y; g.ldc = W; g.sC = (long long)R * W;
+    g.M = R; g.N = W; g.K = R; g.div = (float)(4 * R * W);
+    return gemm(false, g, P, s);
+}
+
+// 2D inverse DCT (idct_inplace) of the top-left h x w block of P planes
+// of coefficients (row stride ldy, plane stride sy) into Z (P planes of
+// h x w, contiguous); U: P h w scratch; Ew, Eh: REDFT01 matrices.
+int idct2d(const float* Y, long long sy, int ldy, int P, int h, int w, const float* Ew, const float* Eh, float* U,
+           float* Z, cudaStream_t s)
+{
+    Gemm g{};
+    // along the rows: U[p][r][n] = sum_k Y[p][r][k] Ew[n][k]
+    g.A = Y; g.lda = ldy; g.sA = sy;
+    g.B = Ew; g.ldb = w; g.sB = 0;
+    g.C = U; g.ldc = w; g.sC = (long long)h * w;
+    g.M = h; g.N = w; g.K = w; g.div = 1.f;
+    int rc = gemm(true, g, P, s);
+    if (rc) return rc;
+    // along the columns: Z[p][m][n] = sum_r Eh[m][r] U[p][r][n]
+    g.A = Eh; g.lda = h; g.sA = 0;
+    g.B = U; g.ldb = w; g.sB = (long long)h * w;
+    g.C = Z; g.ldc = w; g.sC = (long long)h * w;
+    g.M = h; g.N = w; g.K = h; g.div = 1.f;
+    return gemm(false, g, P, s);
+}
+
+int copy_block(float* dst, long long sd, int ldd, const float* src, long long ss, int lds, int P, int bh, int bw,
+               cudaStream_t s)
+{
+    if (bh <= 0 || bw <= 0) return VBM3D_OK;
+    const long long total = (long long)bh * bw;
+    const unsigned bx = (unsigned)std::min<long long>((total + 255) / 256, 1024);
+    copy_block_kernel<<<dim3(bx, (unsigned)P), 256, 0, s>>>(dst, sd, ldd, src, ss, lds, bh, bw);
+    MCK(cudaGetLastError());
+    return VBM3D_OK;
+}
+
+// Rows (or columns) that `for (j = 0; j < n * factor; ++j)` visits for an
+// int n and a float factor: the product and the comparison are in float
+// (recompose.cpp:45-46, merge_coarse.cpp:34-35).
+int block_count(int n, float factor)
+{
+    const volatile float bound = (float)n * factor;
+    int j = 0;
+    while ((float)j < bound) j++;
+    return j;
+}
+
+// Level sizes: halved by integer division per level (decompose.cpp:56-57).
+void level_sizes(int H, int W, int levels, std::vector<int>& hs, std::vector<int>& ws)
+{
+    hs.assign(levels, 0);
+    ws.assign(levels, 0);
+    int h = H, w = W;
+    for (int i = 0; i < levels; i++) {
+        hs[i] = h;
+        ws[i] = w;
+        h /= 2;
+        w /= 2;
+    }
+}
+
+// Cosine matrices for the sizes in `need` (forward or inverse), laid out
+// one after the other in `mats` (offsets returned per size index).
+struct MatSet {
+    std::vector<int> n;
+    std::vector<bool> inv;
+    std::vector<size_t> off;
+    size_t total = 0;
+    int add(int size, bool inverse)
+    {
+        for (size_t i = 0; i < n.size(); i++)
+            if (n[i] == size && inv[i] == inverse) return (int)i;
+        n.push_back(size);
+        inv.push_back(inverse);
+        off.push_back(total);
+        total += (size_t)size * size;
+        return (int)n.size() - 1;
+    }
+};
+
+int check_dims(unsigned width, unsigned height, unsigned planes, unsigned levels)
+{
+    if (!width || !height || !planes || !levels)
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "empty image, no planes or no levels");
+    if (levels > 30 || (height >> (levels - 1)) == 0 || (width >> (levels - 1)) == 0)
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "%u levels leave an empty level of a %ux%u image", levels, width,
+                    height);
+    if ((unsigned long long)planes * height > 8000000ull || width > 65536 || height > 65536)
+        return fail(VBM3D_ERR_UNSUPPORTED, "image stack too large for one call");
+    return VBM3D_OK;
+}
+
+}  // namespace
+}  // namespace ms
+}  // namespace vbm3d
+
+using namespace vbm3d::ms;
+
+extern "C" {
+
+int vbm3d_gpu_ms_decompose(const float* in, unsigned width, unsigned height, unsigned planes, unsigned levels,
+                           float* const* out, void* stream)
+{
+    if (!in || !out) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL pointer");
+    int rc = check_dims(width, height, planes, levels);
+    if (rc) return rc;
+    for (unsigned i = 0; i < levels; i++)
+        if (!out[i]) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL output level %u", i);
+    const int W = (int)width, H = (int)height, P = (int)planes, L = (int)levels;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<int> hs, ws;
+    level_sizes(H, W, L, hs, ws);
+    MatSet ms;
+    const int iDw = ms.add(W, false), iDh = ms.add(H, false);
+    std::vector<int> iEw(L), iEh(L);
+    for (int i = 0; i < L; i++) {
+        iEw[i] = ms.add(ws[i], true);
+        iEh[i] = ms.add(hs[i], true);
+    }
+    const size_t plane = (size_t)P * H * W;
+    Scratch sc;
+    sc.s = s;
+    MCK(cudaMallocAsync(&sc.base, (2 * plane + ms.total) * sizeof(float), s));
+    float* T = sc.base;
+    float* Y = T + plane;
+    float* mats = Y + plane;
+    for (size_t i = 0; i < ms.n.size(); i++)
+        if ((rc = cosine_matrix(mats + ms.off[i], ms.n[i], ms.inv[i], s))) return rc;
+    if ((rc = dct2d(in, P, H, W, mats + ms.off[iDw], mats + ms.off[iDh], T, Y, s))) return rc;
+    for (int i = 0; i < L; i++)
+        if ((rc = idct2d(Y, (long long)H * W, W, P, hs[i], ws[i], mats + ms.off[iEw[i]], mats + ms.off[iEh[i]], T,
+                         out[i], s)))
+            return rc;
+    return VBM3D_OK;
+}
+
+int vbm3d_gpu_ms_recompose(const float* const* levels_in, unsigned width, unsigned height, unsigned planes,
+                           unsigned levels, float factor, float* out, void* stream)
+{
+    if (!levels_in || !out) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL pointer");
+    int rc = check_dims(width, height, planes, levels);
+    if (rc) return rc;
+    for (unsigned i = 0; i < levels; i++)
+        if (!levels_in[i]) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL input level %u", i);
+    if (!(factor <= 1.0f))
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "recompose factor %g > 1 (the reference copies past the level)",
+                    (double)factor);
+    const int W = (int)width, H = (int)height, P = (int)planes, L = (int)levels;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<int> hs, ws;
+    level_sizes(H, W, L, hs, ws);
+    MatSet ms;
+    std::vector<int> iDw(L), iDh(L);
+    for (int i = 0; i < L; i++) {
+        iDw[i] = ms.add(ws[i], false);
+        iDh[i] = ms.add(hs[i], false);
+    }
+    const int iEw = ms.add(W, true), iEh = ms.add(H, true);
+    const size_t plane = (size_t)P * H * W;
+    Scratch sc;
+    sc.s = s;
+    MCK(cudaMallocAsync(&sc.base, (3 * plane + ms.total) * sizeof(float), s));
+    float* T = sc.base;
+    float* Yo = T + plane;
+    float* Yi = Yo + plane;
+    float* mats = Yi + plane;
+    for (size_t i = 0; i < ms.n.size(); i++)
+        if ((rc = cosine_matrix(mats + ms.off[i], ms.n[i], ms.inv[i], s))) return rc;
+    // the DCT of level 0, then each coarser level's low frequencies over it
+    if ((rc = dct2d(levels_in[0], P, H, W, mats + ms.off[iDw[0]], mats + ms.off[iDh[0]], T, Yo, s))) return rc;
+    for (int i = 1; i < L; i++) {
+        const int h = hs[i], w = ws[i];
+        if ((rc = dct2d(levels_in[i], P, h, w, mats + ms.off[iDw[i]], mats + ms.off[iDh[i]], T, Yi, s))) return rc;
+        const int bh = std::min(block_count(h, factor), h), bw = std::min(block_count(w, factor), w);
+        if ((rc = copy_block(Yo, (long long)H * W, W, Yi, (long long)h * w, w, P, bh, bw, s))) return rc;
+    }
+    return idct2d(Yo, (long long)H * W, W, P, H, W, mats + ms.off[iEw], mats + ms.off[iEh], T, out, s);
+}
+
+int vbm3d_gpu_ms_merge_coarse(const float* fine, const float* coarse, unsigned width, unsigned height,
+                              unsigned cwidth, unsigned cheight, unsigned planes, float factor, float* out,
+                              void* stream)
+{
+    if (!fine || !coarse || !out) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL pointer");
+    int rc = check_dims(width, height, planes, 1);
+    if (rc) return rc;
+    if ((rc = check_dims(cwidth, cheight, planes, 1))) return rc;
+    if (!(factor <= 1.0f))
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "merge factor %g > 1 (the reference copies past the coarse image)",
+                    (double)factor);
+    const int W = (int)width, H = (int)height, P = (int)planes, cw = (int)cwidth, ch = (int)cheight;
+    const int bh = block_count(ch, factor), bw = block_count(cw, factor);
+    if (bh > H || bw > W)
+        return fail(VBM3D_ERR_INVALID_ARGUMENT, "coarse block %dx%d larger than the fine image", bw, bh);
+    cudaStream_t s = (cudaStream_t)stream;
+    MatSet ms;
+    const int iDw = ms.add(W, false), iDh = ms.add(H, false), iDcw = ms.add(cw, false), iDch = ms.add(ch, false);
+    const int iEw = ms.add(W, true), iEh = ms.add(H, true);
+    const size_t plane = (size_t)P * H * W, cplane = (size_t)P * ch * cw;
+    Scratch sc;
+    sc.s = s;
+    const size_t big = std::max(plane, cplane);
+    MCK(cudaMallocAsync(&sc.base, (plane + 2 * big + ms.total) * sizeof(float), s));
+    float* Yo = sc.base;
+    float* Yc = Yo + plane;
+    float* T = Yc + big;
+    float* mats = T + big;
+    for (size_t i = 0; i < ms.n.size(); i++)
+        if ((rc = cosine_matrix(mats + ms.off[i], ms.n[i], ms.inv[i], s))) return rc;
+    if ((rc = dct2d(fine, P, H, W, mats + ms.off[iDw], mats + ms.off[iDh], T, Yo, s))) return rc;
+    if ((rc = dct2d(coarse, P, ch, cw, mats + ms.off[iDcw], mats + ms.off[iDch], T, Yc, s))) return rc;
+    if ((rc = copy_block(Yo, (long long)H * W, W, Yc, (long long)ch * cw, cw, P, std::min(bh, ch), std::min(bw, cw),
+                         s)))
+        return rc;
+    return idct2d(Yo, (long long)H * W, W, P, H, W, mats + ms.off[iEw], mats + ms.off[iEh], T, out, s);
+}
+
+}  // extern "C"
