@@ -80,57 +80,87 @@ struct Gemm {
     float div;  // divides every result when != 1
 };
 
-constexpr int BM = 128, BN = 128, BK = 8, kThreads = 256;
+constexpr int BM = 128, BN = 128, BK = 16, kThreads = 256;
+constexpr int AP = BM + 4, BP = BN + 4;  // padded shared rows (16-byte multiples)
+
+// Eight consecutive values row[k .. k+8) (zero past K), as two 16-byte
+// loads when the row is 16-byte aligned (VEC) and the four are in range.
+template <bool VEC>
+__device__ __forceinline__ void load8(const float* __restrict__ row, int k, int K, float* v)
+{
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int kk = k + 4 * h;
+        if (VEC && kk + 3 < K) {
+            const float4 q = __ldg(reinterpret_cast<const float4*>(row + kk));
+            v[4 * h] = q.x;
+            v[4 * h + 1] = q.y;
+            v[4 * h + 2] = q.z;
+            v[4 * h + 3] = q.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) v[4 * h + i] = kk + i < K ? __ldg(row + kk + i) : 0.f;
+        }
+    }
+}
 
 // C[b] = A[b] op(B[b]) (op(B) = B^T when BT) in float with FMA, one
 // 128 x 128 tile per block; each thread owns rows {4ty..4ty+3, 64+4ty..}
-// and columns {4tx..4tx+3, 64+4tx..} of the tile.  The next K slice is
-// loaded into registers while the current one is multiplied from shared
-// memory (two stages, one barrier per slice).
-template <bool BT>
-__global__ void __launch_bounds__(kThreads) gemm_kernel(const Gemm g)
+// and columns {4tx..4tx+3, 64+4tx..} of the tile.  The next K slice of 16
+// is loaded into registers while the current one is multiplied from shared
+// memory (two stages, one barrier per slice).  Loaders: A (and B^T) one
+// row per lane (rows t mod 128, K half t / 128), stored transposed without
+// bank conflicts; B one K row per 16 lanes.  VA / VB: 16-byte loads (the
+// operand's rows are 16-byte aligned).
+template <bool BT, bool VA, bool VB>
+__global__ void __launch_bounds__(kThreads, 2) gemm_kernel(const Gemm g)
 {
-    __shared__ __align__(16) float As[2][BK][BM];
-    __shared__ __align__(16) float Bs[2][BK][BN];
+    __shared__ __align__(16) float As[2][BK][AP];
+    __shared__ __align__(16) float Bs[2][BK][BP];
     const long long b = blockIdx.z;
     const float* __restrict__ A = g.A + b * g.sA;
     const float* __restrict__ B = g.B + b * g.sB;
     float* __restrict__ C = g.C + b * g.sC;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int t = threadIdx.x;
-    // loaders: A (and B^T) rows t / 2, four K columns from (t & 1) * 4;
-    // B: K row t / 32, four N columns from (t & 31) * 4
-    const int lr = t >> 1, lk = (t & 1) * 4;
-    const int bk = t >> 5, bn = (t & 31) * 4;
-    float ra[4], rb[4];
+    const int lr = t & 127, lk = (t >> 7) * 8;
+    const int bk = t >> 4, bn = (t & 15) * 8;
+    float ra[8], rb[8];
     auto load = [&](int k0) {
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int m = m0 + lr, k = k0 + lk + i;
-            ra[i] = (m < g.M && k < g.K) ? A[(long long)m * g.lda + k] : 0.f;
-        }
-        if (BT) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int n = n0 + lr, k = k0 + lk + i;
-                rb[i] = (n < g.N && k < g.K) ? B[(long long)n * g.ldb + k] : 0.f;
-            }
+        const int m = m0 + lr;
+        if (m < g.M) {
+            load8<VA>(A + (long long)m * g.lda, k0 + lk, g.K, ra);
         } else {
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int k = k0 + bk, n = n0 + bn + i;
-                rb[i] = (k < g.K && n < g.N) ? B[(long long)k * g.ldb + n] : 0.f;
+            for (int i = 0; i < 8; i++) ra[i] = 0.f;
+        }
+        if (BT) {
+            const int n = n0 + lr;
+            if (n < g.N) {
+                load8<VB>(B + (long long)n * g.ldb, k0 + lk, g.K, rb);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++) rb[i] = 0.f;
+            }
+        } else {
+            const int k = k0 + bk;
+            if (k < g.K) {
+                load8<VB>(B + (long long)k * g.ldb + n0, bn, g.N - n0, rb);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++) rb[i] = 0.f;
             }
         }
     };
     auto store = [&](int s) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) As[s][lk + i][lr] = ra[i];
+        for (int i = 0; i < 8; i++) As[s][lk + i][lr] = ra[i];
         if (BT) {
 #pragma unroll
-            for (int i = 0; i < 4; i++) Bs[s][lk + i][lr] = rb[i];
+            for (int i = 0; i < 8; i++) Bs[s][lk + i][lr] = rb[i];
         } else {
             *reinterpret_cast<float4*>(&Bs[s][bk][bn]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+            *reinterpret_cast<float4*>(&Bs[s][bk][bn + 4]) = make_float4(rb[4], rb[5], rb[6], rb[7]);
         }
     };
     const int tx = t & 15, ty = t >> 4;
@@ -199,8 +229,24 @@ int gemm(bool bt, const Gemm& g, int batch, cudaStream_t s)
     if (g.M <= 0 || g.N <= 0 || g.K <= 0 || batch <= 0) return VBM3D_OK;
     const dim3 grid((unsigned)((g.N + BN - 1) / BN), (unsigned)((g.M + BM - 1) / BM), (unsigned)batch);
     if (grid.y > 65535u || grid.z > 65535u) return fail(VBM3D_ERR_UNSUPPORTED, "matrix product too large");
-    if (bt) gemm_kernel<true><<<grid, kThreads, 0, s>>>(g);
-    else gemm_kernel<false><<<grid, kThreads, 0, s>>>(g);
+    // 16-byte loads: every row of the operand starts on a 16-byte boundary
+    auto rows16 = [](const float* p, int ld, long long sb) {
+        return ((uintptr_t)p & 15) == 0 && (ld & 3) == 0 && (sb & 3) == 0;
+    };
+    const bool va = rows16(g.A, g.lda, g.sA), vb = rows16(g.B, g.ldb, g.sB);
+#define MS_GEMM(BT_, VA_, VB_) gemm_kernel<BT_, VA_, VB_><<<grid, kThreads, 0, s>>>(g)
+    if (bt) {
+        if (va && vb) MS_GEMM(true, true, true);
+        else if (va) MS_GEMM(true, true, false);
+        else if (vb) MS_GEMM(true, false, true);
+        else MS_GEMM(true, false, false);
+    } else {
+        if (va && vb) MS_GEMM(false, true, true);
+        else if (va) MS_GEMM(false, true, false);
+        else if (vb) MS_GEMM(false, false, true);
+        else MS_GEMM(false, false, false);
+    }
+#undef MS_GEMM
     MCK(cudaGetLastError());
     return VBM3D_OK;
 }

@@ -14,6 +14,12 @@ filtering of step 1 per table set, mid, the same for step 2, final), then
 once more through vbm3d_batch_profile, which prints each work launch.
 TV-L1: forward and backward flows of a one-channel clip with the options of
 the reference's flow scripts (vbm3d_gpu_tvl1_video), run twice.
+Multiscaler (--ms LEVELS): the DCT pyramid of a clip (vbm3d_gpu_ms_decompose)
+and its recomposition with ratio 0.7 (vbm3d_gpu_ms_recompose), run
+`--runs` times; launch order per run: cosine matrices, the forward
+transform's two products, two products per level; then the recomposition's
+cosine matrices, per level two products (and a block copy from level 1),
+the inverse transform's two products.
 """
 import argparse
 
@@ -37,7 +43,16 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="batched form over this many clips")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--tvl1", action="store_true", help="TV-L1 flows of a one-channel clip")
+    ap.add_argument("--ms", type=int, default=0, help="multiscaler DCT pyramid with this many levels")
     a = ap.parse_args()
+    if a.ms:
+        _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
+        x = torch.from_numpy(noisy).cuda()
+        for _ in range(a.runs):
+            vb.ms_recompose(vb.ms_decompose(x, a.ms), 0.7)
+        torch.cuda.synchronize()
+        print("ok")
+        return
     if a.tvl1:
         _, noisy, _, _ = make_clip(a.width, a.height, a.frames, 1, a.sigma, seed=4000, vmax=6.0)
         v = torch.from_numpy(noisy[:, 0].copy()).cuda()
