@@ -48,6 +48,8 @@ W, H, F, C = 1920, 1080, 30, 3
 SIGMA = 30.0
 SEED = 3000
 WORKLOAD_1080 = "plain VBM3D, RGB 1920x1080x30, sigma=30, reference default parameters, colour transform on, no flow"
+WORKLOAD_MS = ("multiscaler DCT pyramid of an RGB 1920x1080x30 clip, 3 levels: decompose, then recompose with "
+               "ratio 0.7 (the multiscale script's pre- and post-processing)")
 WORKLOAD_BATCH = ("batched VBM3D, 64 clips: width U[160,1280], height U[120,720], 5-40 frames, 1 or 3 channels, "
                   "sigma in {5,10,20,30,50}; reference default parameters, colour transform on, no flow")
 
@@ -269,6 +271,44 @@ def timed(stream, fn, steps):
     return e0.elapsed_time(e1) / steps
 
 
+def measure_multiscaler(vb, dev, stream, clocks, with_cpu):
+    """The multiscaler DCT pyramid (vbm3d_gpu_ms_decompose / _recompose) of an
+    RGB 1080p30 clip, 3 levels; its float products against the nominal FP32
+    FMA rate; optionally the restatement (scipy, double) on one frame."""
+    import torch
+    F_, C_, H_, W_, L_ = 30, 3, 1080, 1920, 3
+    g = torch.Generator(device=dev).manual_seed(5)
+    x = torch.rand((F_, C_, H_, W_), device=dev, generator=g) * 255
+    lv = vb.ms_decompose(x, L_)
+    for _ in range(3):
+        vb.ms_recompose(vb.ms_decompose(x, L_), 0.7)
+    t_dec = timed(stream, lambda: vb.ms_decompose(x, L_), 3)
+    t_rec = timed(stream, lambda: vb.ms_recompose(lv, 0.7), 3)
+    P_ = F_ * C_
+    # multiply-adds of the products: a 2D transform of R x W costs
+    # R W (W + R) per plane; decompose and recompose each run one full-size
+    # transform and one transform per level
+    full = P_ * H_ * W_ * (W_ + H_)
+    levels = sum(P_ * (H_ >> i) * (W_ >> i) * ((W_ >> i) + (H_ >> i)) for i in range(L_))
+    macs = 2.0 * (full + levels)
+    ms = t_dec + t_rec
+    peak, src = fp32_peak(dev, clocks)
+    tf = 2 * macs / (ms / 1e3) / 1e12
+    out = {"workload": WORKLOAD_MS, "value": round(F_ * H_ * W_ / 1e6 / (ms / 1e3), 3), "unit": "Mpix-frames/s",
+           "decompose_ms": round(t_dec, 2), "recompose_ms": round(t_rec, 2), "tflops": round(tf, 1),
+           "fp32_frac": round(tf / peak, 3), "fp32_peak_source": src}
+    if with_cpu:
+        from oracle import ms_oracle
+        img = x[0].cpu().numpy()
+        t0 = time.perf_counter()
+        ms_oracle.recompose(ms_oracle.decompose(img, L_), 0.7)
+        dt = time.perf_counter() - t0
+        out["cpu_port"] = {"value": round(H_ * W_ / 1e6 / dt, 3), "unit": "Mpix-frames/s", "cores": 1,
+                           "kind": "port", "sample": "one RGB frame through oracle/ms_oracle.py (scipy FFT DCTs "
+                                                     "in double)"}
+    return out
+
+
 def measure_1080(vb, dev, steps, warmup, full):
     """The plain 1080p30 workload; with full, also the roofline inputs."""
     import torch
@@ -419,6 +459,10 @@ def run_gpu(args):
                           "unit": UNIT, "ms_per_step": round(ms1080, 1),
                           "psnr_final": round(psnr(clean, out["bf"][1].cpu().numpy()), 3)}
 
+        extra_ms = None
+        if not args.no_1080p:
+            extra_ms = measure_multiscaler(vb, dev, stream, clocks, rank == 0 and not args.no_cpu_baseline)
+
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
             samples, desc = cpu_sample("batch64", clips=clips)
@@ -437,7 +481,7 @@ def run_gpu(args):
                        "create_s": round(create_s, 2),
                        "psnr_gain_db": {"min": round(min(gain), 3), "mean": round(float(np.mean(gain)), 3)}},
             "plain": plain, "clocks": clocks, "e2e": e2e, "gpu_launches": gpu_launches, "roofline": roofline,
-            "cpu_baseline": cpu, "plain_1080p30": extra_1080,
+            "cpu_baseline": cpu, "plain_1080p30": extra_1080, "multiscaler_1080p30": extra_ms,
             "launches": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in l.items()
                           if k in ("phase", "k", "channels", "clips", "refs", "ms")} for l in launches],
         }
