@@ -186,7 +186,7 @@ struct ClipHost {
 struct WorkLaunch {
     int phase = 0, cls = 0;
     std::vector<int> clips;  // batch indices, in cost order; slot = position
-    std::vector<unsigned char> table;  // block matching: its BmTable, passed by value
+    std::vector<unsigned char> table;  // passed by value: block matching its BmTable, filtering its tables
     int ws = 0;              // per-warp workspace (bm: bytes, filter: floats)
     uint4* d_items = nullptr;
     unsigned nitems = 0;
@@ -493,7 +493,12 @@ void plan_launches(vbm3d_batch& b)
             for (int c : b.order) {
                 const StepHead& P = b.ch[c].h[s];
                 if (class_of(ph, P) != cls) continue;
-                if (!(ph & 1) && (int)w.clips.size() == kTableClips) {  // a full table: next launch
+                // a full table, or (filtering) transform tables other than the
+                // launch's: next launch
+                const bool next = !(ph & 1) ? (int)w.clips.size() == kTableClips
+                                            : !w.clips.empty() && memcmp(&b.ch[w.clips[0]].t[s], &b.ch[c].t[s],
+                                                                         sizeof(CompactTables)) != 0;
+                if (next) {
                     b.work[ph].push_back(w);
                     w.clips.clear();
                     w.ws = 0;
@@ -608,6 +613,12 @@ int allocate(vbm3d_batch& b, cudaStream_t s)
         h.tab_idx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 3]);
         h.tab_nsx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 4]);
     }
+    // filtering: the transform tables every clip of the launch shares
+    for (int ph = 1; ph < kPhases; ph += 2)
+        for (WorkLaunch& w : b.work[ph]) {
+            w.table.assign(sizeof(CompactTables), 0);
+            memcpy(w.table.data(), &b.ch[w.clips[0]].t[ph / 2], sizeof(CompactTables));
+        }
     // block-matching tables: parameters and buffers of each launch's clips
     for (int ph = 0; ph < kPhases; ph += 2)
         for (WorkLaunch& w : b.work[ph]) {

@@ -39,9 +39,14 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // w + warps, ...), so at any time a block works on neighbouring reference
 // patches whose search windows and groups overlap in L1, as a block of the
 // plain kernel does.  Block matching reads its clips' parameters from the
-// launch's kernel-argument table (batch.cuh); filtering keeps its current
-// clip's parameters and tables in shared memory, reloaded when an item of
-// another clip comes up.
+// launch's kernel-argument table (batch.cuh).  Filtering keeps its current
+// clip's scalar parameters in shared memory, reloaded when an item of
+// another clip comes up; for k = 8 it reads the transform tables of its
+// class (the same for every clip of the launch) from its kernel arguments,
+// so each table entry is a constant-bank operand of the transforms' FMAs
+// (-7 % to -16 % per launch), while for k = 7 that form needs more than its
+// 128 registers and spills (+25 % to +40 %), so k = 7 reads the tables from
+// the shared-memory copy.
 
 template <int STEP, int K, int C>
 __global__ void __maxnreg__(C == 3 ? 96 : 80)  // as bm2_kernel
@@ -71,7 +76,7 @@ batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ i
 template <int STEP, int K>
 __global__ void __launch_bounds__(256, 2)
 batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
-                    unsigned* __restrict__ head, int warp_floats)
+                    unsigned* __restrict__ head, int warp_floats, const __grid_constant__ CompactTables T)
 {
     extern __shared__ __align__(16) float fsm[];
     __shared__ uint4 s_item[2];
@@ -87,14 +92,19 @@ batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict
         claim_item(items, nitems, head, &s_item[buf ^ 1]);
         const BatchClip& B = clips[I.x];
         if (I.x != cur) {
-            copy_words(V, &B.s[STEP - 1].v, (int)sizeof(FilterView));
+            if (K == 8) copy_words(&V->h, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
+            else copy_words(V, &B.s[STEP - 1].v, (int)sizeof(FilterView));
             __syncthreads();
             cur = I.x;
         }
         const AggTarget A{nullptr, nullptr, B.pair};
         for (unsigned j = wid; j < I.z; j += nwarps) {
-            filter_ref<STEP, K, true>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                      B.tab_nsx, A);
+            if (K == 8)
+                filter_ref<STEP, K, true>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                          B.tab_nsx, A);
+            else
+                filter_ref<STEP, K, true>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                          B.tab_nsx, A);
             __syncwarp();
         }
         __syncthreads();
