@@ -381,9 +381,14 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
     if (STEP == 2) gather_k<K, SS>(P, basic, idx, nsx, log2n, gB, lane);
     cp_async_wait_all();
     __syncwarp();
-    // 2D transforms, one slice (c, n) per lane, in registers
+    // 2D transforms, one slice (c, n) per lane, in registers; the barrier
+    // keeps the compiler from interleaving the two groups' transforms (two
+    // blocks of k*k registers live at once)
     slice_fwd<K, SS>(P, T, gA, nsl, lane);
-    if (STEP == 2) slice_fwd<K, SS>(P, T, gB, nsl, lane);
+    if (STEP == 2) {
+        __syncwarp();
+        slice_fwd<K, SS>(P, T, gB, nsl, lane);
+    }
     __syncwarp();
 
     float wgt[kMaxC];
