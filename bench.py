@@ -285,12 +285,20 @@ def measure_multiscaler(vb, dev, stream, clocks, with_cpu):
     t_dec = timed(stream, lambda: vb.ms_decompose(x, L_), 3)
     t_rec = timed(stream, lambda: vb.ms_recompose(lv, 0.7), 3)
     P_ = F_ * C_
-    # multiply-adds of the products: a 2D transform of R x W costs
-    # R W (W + R) per plane; decompose and recompose each run one full-size
-    # transform and one transform per level
-    full = P_ * H_ * W_ * (W_ + H_)
-    levels = sum(P_ * (H_ >> i) * (W_ >> i) * ((W_ >> i) + (H_ >> i)) for i in range(L_))
-    macs = 2.0 * (full + levels)
+    # multiply-adds of the products: every transform is split into its even
+    # and odd halves (ne = ceil(n / 2), no = n / 2): a forward 2D transform
+    # of R x W costs R (ne_W^2 + no_W^2) + W (ne_R^2 + no_R^2) per plane, an
+    # inverse one R ne_W W + W ne_R R; decompose runs one full-size forward
+    # transform and one inverse per level, recompose one forward per level
+    # and one full-size inverse
+    def fwd(r, w):
+        return P_ * (r * (((w + 1) // 2) ** 2 + (w // 2) ** 2) + w * (((r + 1) // 2) ** 2 + (r // 2) ** 2))
+
+    def inv(r, w):
+        return P_ * (r * ((w + 1) // 2) * w + w * ((r + 1) // 2) * r)
+
+    lv = [(H_ >> i, W_ >> i) for i in range(L_)]
+    macs = float(fwd(H_, W_) + sum(inv(r, w) for r, w in lv) + sum(fwd(r, w) for r, w in lv) + inv(H_, W_))
     ms = t_dec + t_rec
     peak, src = fp32_peak(dev, clocks)
     tf = 2 * macs / (ms / 1e3) / 1e12
