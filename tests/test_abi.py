@@ -158,3 +158,20 @@ def test_tvl1_rejects_bad_options_before_any_cuda_call(lib):
         assert lib.vbm3d_gpu_tvl1_pairs(fake, fake, 1, 64, 48, C.byref(q), fake, None, None) == 1
     assert lib.vbm3d_gpu_tvl1_pairs(fake, fake, 0, 64, 48, C.byref(p), fake, None, None) == 1
     assert lib.vbm3d_gpu_tvl1_video(fake, 64, 48, 1, C.byref(p), fake, fake, None) == 1
+
+
+def test_multiscaler_rejects_bad_arguments_before_any_cuda_call(lib):
+    fake = C.c_void_p(16)
+    outs = (C.c_void_p * 3)(fake, fake, fake)
+    # an empty level (8 >> 4 == 0), no planes, no levels, a NULL output level
+    assert lib.vbm3d_gpu_ms_decompose(fake, 8, 8, 1, 5, outs, None) == 1
+    assert lib.vbm3d_gpu_ms_decompose(fake, 8, 8, 0, 1, outs, None) == 1
+    assert lib.vbm3d_gpu_ms_decompose(fake, 8, 8, 1, 0, outs, None) == 1
+    assert lib.vbm3d_gpu_ms_decompose(fake, 8, 8, 1, 3, (C.c_void_p * 3)(fake, None, fake), None) == 1
+    assert lib.vbm3d_gpu_ms_decompose(None, 8, 8, 1, 1, outs, None) == 1
+    # a recomposition ratio above 1 would make the reference copy past the level
+    assert lib.vbm3d_gpu_ms_recompose(outs, 8, 8, 1, 2, C.c_float(1.5), fake, None) == 1
+    assert lib.vbm3d_gpu_ms_recompose(outs, 8, 8, 1, 2, C.c_float(float("nan")), fake, None) == 1
+    # a coarse block larger than the fine image
+    assert lib.vbm3d_gpu_ms_merge_coarse(fake, fake, 8, 8, 16, 16, 1, C.c_float(0.9), fake, None) == 1
+    assert lib.vbm3d_gpu_ms_merge_coarse(fake, None, 8, 8, 4, 4, 1, C.c_float(0.5), fake, None) == 1
