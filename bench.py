@@ -185,19 +185,24 @@ class ClockSampler:
 
 
 def dist_setup(n):
+    """One process per GPU (torchrun's RANK / WORLD_SIZE / MASTER_*): NCCL on
+    GPUs, gloo where there is none (the CPU tests of the replica path)."""
     if n <= 1:
         return 0, 1
+    import torch
     import torch.distributed as dist
-    dist.init_process_group("nccl")
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return dist.get_rank(), dist.get_world_size()
 
 
 def reduce_max(x, world):
+    """The largest of the ranks' values (timings: the slowest replica)."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
