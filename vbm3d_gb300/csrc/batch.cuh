@@ -76,13 +76,14 @@ static_assert(sizeof(BmTable) <= 31 * 1024, "kernel parameter limit");
 
 // Work phases and kernel classes: block matching has one class per
 // (k, C) in {7, 8} x {1, 3}; filtering one per transform table set,
-// (k, T_2D) in {(7, DCT), (8, DCT), (8, bior1.5)}.
+// (k, T_2D) in {(7, DCT), (8, DCT), (8, bior1.5)}, and channel count (one
+// channel: the shared-slice transforms, four lanes per slice; classes 3-5).
 constexpr int kPhases = 4;   // bm1, filter1, bm2, filter2
-constexpr int kClasses = 4;
+constexpr int kClasses = 6;
 
 inline int class_of(int phase, const StepHead& P)
 {
-    if (phase & 1) return P.k == 8 ? (P.T2D == kBIOR ? 2 : 1) : 0;
+    if (phase & 1) return (P.k == 8 ? (P.T2D == kBIOR ? 2 : 1) : 0) + (P.C == 1 ? 3 : 0);
     return (P.k == 8 ? 2 : 0) + (P.C == 3 ? 1 : 0);
 }
 

@@ -73,7 +73,7 @@ batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ i
     }
 }
 
-template <int STEP, int K>
+template <int STEP, int K, int LPS>
 __global__ void __launch_bounds__(256, 2)
 batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
                     unsigned* __restrict__ head, int warp_floats, const __grid_constant__ CompactTables T)
@@ -100,11 +100,11 @@ batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict
         const AggTarget A{nullptr, nullptr, B.pair};
         for (unsigned j = wid; j < I.z; j += nwarps) {
             if (K == 8)
-                filter_ref<STEP, K, true>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                          B.tab_nsx, A);
+                filter_ref<STEP, K, true, LPS>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                               B.tab_nsx, A);
             else
-                filter_ref<STEP, K, true>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                          B.tab_nsx, A);
+                filter_ref<STEP, K, true, LPS>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                               B.tab_nsx, A);
             __syncwarp();
         }
         __syncthreads();

@@ -18,9 +18,12 @@ const void* work_kernel_step1(int phase, int cls)
     }
     if (phase == 1) {
         switch (cls) {
-            case 0: return reinterpret_cast<const void*>(batch_filter_kernel<1, 7>);
-            case 1:  // DCT and bior1.5 tables share the k = 8 kernel
-            case 2: return reinterpret_cast<const void*>(batch_filter_kernel<1, 8>);
+            case 0: return reinterpret_cast<const void*>(batch_filter_kernel<1, 7, 1>);
+            case 1:  // DCT and bior1.5 tables share the k = 8 kernels
+            case 2: return reinterpret_cast<const void*>(batch_filter_kernel<1, 8, 1>);
+            case 3: return reinterpret_cast<const void*>(batch_filter_kernel<1, 7, 4>);  // one channel
+            case 4:
+            case 5: return reinterpret_cast<const void*>(batch_filter_kernel<1, 8, 4>);
             default: return nullptr;
         }
     }

@@ -242,7 +242,7 @@ filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const
     }
 }
 
-template <int STEP, int K, bool PAIR>
+template <int STEP, int K, bool PAIR, int LPS>
 __global__ void __launch_bounds__(128, 4)
 filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
                 const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx, const AggTarget A,
@@ -252,25 +252,36 @@ filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
     if (r >= P.nrefs) return;
-    filter_ref<STEP, K, PAIR>(P, P, r, fsm + (size_t)wid * warp_floats, lane, noisy, basic, tab_idx, tab_nsx, A);
+    filter_ref<STEP, K, PAIR, LPS>(P, P, r, fsm + (size_t)wid * warp_floats, lane, noisy, basic, tab_idx, tab_nsx,
+                                   A);
 }
 
 namespace {
 
-template <int STEP, int K, bool PAIR>
-cudaError_t launch_k(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
-                     const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+template <int STEP, int K, bool PAIR, int LPS>
+cudaError_t launch_k_mode(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                          const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
 {
     const int warps = 4;
     const int wf = kMaxN + (STEP == 1 ? 1 : 2) * P.C * P.N * (K * K + 1);
     const size_t smem = (size_t)warps * wf * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR>,
+    cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR, LPS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (count + warps - 1) / warps;
-    filter_kernel_k<STEP, K, PAIR><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
-                                                                                  tab_nsx, A, wf);
+    filter_kernel_k<STEP, K, PAIR, LPS><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
+                                                                                       tab_nsx, A, wf);
     return cudaGetLastError();
+}
+
+// One-channel groups (at most N <= 8 slices) take the shared-slice
+// transforms, four lanes per slice; others one slice per lane.
+template <int STEP, int K, bool PAIR>
+cudaError_t launch_k(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                     const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+{
+    if (P.C == 1) return launch_k_mode<STEP, K, PAIR, 4>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    return launch_k_mode<STEP, K, PAIR, 1>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
 }
 
 template <int STEP, bool PAIR>

@@ -191,6 +191,167 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepHead& P, const T
     }
 }
 
+// ------------------------------------------------------ shared slices ---
+// The same 2D transforms with LPS lanes per slice, for groups of at most
+// 32 / LPS slices (filter_ref uses LPS = 4 for one-channel groups, which
+// have at most 8): lane `part` of a
+// slice owns its rows part, part + LPS, ... in the row pass and the same
+// columns in the column pass.  Every output is the same sum as in row_pass
+// / col_pass, over the same terms in the same order with the same
+// rounding, so the results are bit-identical; the passes go through the
+// slice in shared memory with a warp barrier between them, and a pass whose
+// stores cross the lanes' lines (bior1.5's transposed outputs) computes all
+// of its lines before any store.
+
+template <int K, bool EXACT>
+__device__ __forceinline__ float row_dot(const float* xr, const float* M, int v)
+{
+    float m = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; j++) m = EXACT ? m + xr[j] * M[v * K + j] : __fmaf_rn(xr[j], M[v * K + j], m);
+    return m;
+}
+template <int K, bool EXACT>
+__device__ __forceinline__ float col_dot(const float* xc, const float* M, int u)
+{
+    float m = 0.f;
+#pragma unroll
+    for (int i = 0; i < K; i++) m = EXACT ? m + xc[i] * M[u * K + i] : __fmaf_rn(M[u * K + i], xc[i], m);
+    return m;
+}
+
+// Row pass of the owned rows (in place; optional elementwise scale of the
+// inputs first), and column pass of the owned columns into out[t][u].
+template <int K, int LPS, bool EXACT>
+__device__ __forceinline__ void rows_owned(float* s, int part, const float* M, const float* pre)
+{
+#pragma unroll
+    for (int t = 0; t < (K + LPS - 1) / LPS; t++) {
+        const int i = part + LPS * t;
+        if (i >= K) continue;
+        float xr[K], y[K];
+#pragma unroll
+        for (int j = 0; j < K; j++) xr[j] = pre ? s[i * K + j] * pre[i * K + j] : s[i * K + j];
+#pragma unroll
+        for (int v = 0; v < K; v++) y[v] = row_dot<K, EXACT>(xr, M, v);
+#pragma unroll
+        for (int v = 0; v < K; v++) s[i * K + v] = y[v];
+    }
+}
+template <int K, int LPS, bool EXACT>
+__device__ __forceinline__ void cols_owned(const float* s, int part, const float* M, float (&out)[(K + LPS - 1) / LPS][K])
+{
+#pragma unroll
+    for (int t = 0; t < (K + LPS - 1) / LPS; t++) {
+        const int j = part + LPS * t;
+        if (j >= K) continue;
+        float xc[K];
+#pragma unroll
+        for (int i = 0; i < K; i++) xc[i] = s[i * K + j];
+#pragma unroll
+        for (int u = 0; u < K; u++) out[t][u] = col_dot<K, EXACT>(xc, M, u);
+    }
+}
+
+// slice_fwd2d over slices g + sl * SS, sl < nsl <= 32 / LPS.
+template <int K, int LPS, int SS, class TT>
+__device__ __forceinline__ void slices_fwd2d_shared(float* g, int nsl, int lane, const StepHead& P, const TT& T)
+{
+    constexpr int NL = (K + LPS - 1) / LPS;
+    const int sl = lane / LPS, part = lane % LPS;
+    const bool act = sl < nsl;
+    float* s = g + sl * SS;
+    const bool bior = K == 8 && P.T2D == kBIOR;
+    float out[NL][K];
+    if (act) {
+        if (bior) rows_owned<K, LPS, true>(s, part, T.fwd, nullptr);
+        else rows_owned<K, LPS, false>(s, part, T.fwd, nullptr);
+    }
+    __syncwarp();
+    if (act) {
+        if (bior) cols_owned<K, LPS, true>(s, part, T.fwd, out);
+        else cols_owned<K, LPS, false>(s, part, T.fwd, out);
+    }
+    __syncwarp();  // every column read before the (transposed) stores
+    if (act) {
+#pragma unroll
+        for (int t = 0; t < NL; t++) {
+            const int j = part + LPS * t;
+            if (j >= K) continue;
+#pragma unroll
+            for (int u = 0; u < K; u++) {
+                if (bior) s[j * K + u] = out[t][u];  // out[u][j] stored transposed
+                else s[u * K + j] = out[t][u] * T.cn[u * K + j];
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// slice_inv2d over slices g + sl * SS, sl < nsl <= 32 / LPS.
+template <int K, int LPS, int SS, class TT>
+__device__ __forceinline__ void slices_inv2d_shared(float* g, int nsl, int lane, const StepHead& P, const TT& T)
+{
+    constexpr int NL = (K + LPS - 1) / LPS;
+    const int sl = lane / LPS, part = lane % LPS;
+    const bool act = sl < nsl;
+    float* s = g + sl * SS;
+    float out[NL][K];
+    if (K == 8 && P.T2D == kBIOR) {
+        // column pass first (each lane stores its own columns), then the row
+        // pass with transposed stores
+        if (act) cols_owned<K, LPS, true>(s, part, T.inv, out);
+        __syncwarp();
+        if (act) {
+#pragma unroll
+            for (int t = 0; t < NL; t++) {
+                const int j = part + LPS * t;
+                if (j >= K) continue;
+#pragma unroll
+                for (int u = 0; u < K; u++) s[u * K + j] = out[t][u];
+            }
+        }
+        __syncwarp();
+        if (act) {
+#pragma unroll
+            for (int t = 0; t < NL; t++) {
+                const int i = part + LPS * t;
+                if (i >= K) continue;
+                float xr[K];
+#pragma unroll
+                for (int j = 0; j < K; j++) xr[j] = s[i * K + j];
+#pragma unroll
+                for (int v = 0; v < K; v++) out[t][v] = row_dot<K, true>(xr, T.inv, v);
+            }
+        }
+        __syncwarp();  // every row read before the transposed stores
+        if (act) {
+#pragma unroll
+            for (int t = 0; t < NL; t++) {
+                const int i = part + LPS * t;
+                if (i >= K) continue;
+#pragma unroll
+                for (int v = 0; v < K; v++) s[v * K + i] = out[t][v];
+            }
+        }
+    } else {
+        if (act) rows_owned<K, LPS, false>(s, part, T.inv, T.cni);
+        __syncwarp();
+        if (act) cols_owned<K, LPS, false>(s, part, T.inv, out);
+        const float coef = 1.0f / (float)(K * 2);
+        if (act) {
+#pragma unroll
+            for (int t = 0; t < NL; t++) {
+                const int j = part + LPS * t;
+                if (j >= K) continue;
+#pragma unroll
+                for (int u = 0; u < K; u++) s[u * K + j] = coef * out[t][u];
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // Gathers the nsx patches of every channel into slices [c][n][K*K] of
 // stride SS, lanes over consecutive pixels (each patch row is contiguous in
 // memory, so a warp load touches a few rows instead of 32 patches).  idx[n]
@@ -358,7 +519,7 @@ __device__ __forceinline__ void slice_fwd(const StepHead& P, const TT& T, float*
 // register-resident transforms for compile-time K (kt == 1, N <= 8), with
 // the warp's shared-memory region `base`.  T holds the kaiser / fwd / inv /
 // cn / cni tables (StepParams, or the batched form's compact copy).
-template <int STEP, int K, bool PAIR, class TT>
+template <int STEP, int K, bool PAIR, int LPS, class TT>
 __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long long r, float* base, int lane,
                                            const float* __restrict__ noisy, const float* __restrict__ basic,
                                            const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
@@ -381,23 +542,36 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
     if (STEP == 2) gather_k<K, SS>(P, basic, idx, nsx, log2n, gB, lane);
     cp_async_wait_all();
     __syncwarp();
-    // 2D transforms, one slice (c, n) per lane, in registers; the barrier
-    // keeps the compiler from interleaving the two groups' transforms (two
+    // 2D transforms: one slice (c, n) per lane in registers (LPS == 1), or
+    // 4 lanes per slice through shared memory (LPS == 4: groups of at most 8
+    // slices, such as every one-channel group; the kernels are instantiated
+    // per mode, so each carries one form's registers); the barrier keeps the
+    // compiler from interleaving the two groups' register transforms (two
     // blocks of k*k registers live at once)
-    slice_fwd<K, SS>(P, T, gA, nsl, lane);
-    if (STEP == 2) {
+    static_assert(LPS == 1 || LPS == 4, "slice modes");
+    if (LPS == 4) {
+        slices_fwd2d_shared<K, 4, SS>(gA, nsl, lane, P, T);
+        if (STEP == 2) slices_fwd2d_shared<K, 4, SS>(gB, nsl, lane, P, T);
+    } else {
+        slice_fwd<K, SS>(P, T, gA, nsl, lane);
+        if (STEP == 2) {
+            __syncwarp();
+            slice_fwd<K, SS>(P, T, gB, nsl, lane);
+        }
         __syncwarp();
-        slice_fwd<K, SS>(P, T, gB, nsl, lane);
     }
-    __syncwarp();
 
     float wgt[kMaxC];
     group_1d<STEP, 8>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
 
-    // inverse 2D, one slice per lane
+    // inverse 2D, as the forward one
     float* ge = STEP == 1 ? gA : gB;
-    for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(ge + sl * SS, P, T);
-    __syncwarp();
+    if (LPS == 4) {
+        slices_inv2d_shared<K, 4, SS>(ge, nsl, lane, P, T);
+    } else {
+        for (int sl = lane; sl < nsl; sl += 32) slice_inv2d<K>(ge + sl * SS, P, T);
+        __syncwarp();
+    }
 
     // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
     const int total = nsl * K2;
