@@ -239,7 +239,9 @@ typedef struct vbm3d_clip {
 } vbm3d_clip;
 
 /* Per phase (block matching / filtering of each step): reference patches
- * per work item and warps per block; 0 and 0 = autotune.  no_graph = 1
+ * per work item and warps per block; 0 and 0 = autotune.  Block matching of
+ * one-channel clips runs two reference patches per warp, and its items hold
+ * twice the tile, so every warp has the same work.  no_graph = 1
  * enqueues the kernels at each run instead of launching the graph.  The
  * last three fields are outputs of vbm3d_batch_get_config. */
 typedef struct vbm3d_batch_config {

@@ -245,13 +245,17 @@ double ref_cost(const StepHead& P)
     return kk * (P.Ns * P.Ns + 2.0 * P.Nf * P.Nb * P.Npr * P.Npr);
 }
 
+int bm_groups_per_warp(int cls);
+
 // Items of one launch: tiles of `tile` consecutive references inside one
-// frame, clips in cost order.  With stride > 1 only every stride-th item
-// is kept (the autotuner's sample).
+// frame (times the groups per warp for block matching: a block's groups
+// all take part in an item), clips in cost order.  With stride > 1 only
+// every stride-th item is kept (the autotuner's sample).
 std::vector<uint4> make_items(const vbm3d_batch& b, const WorkLaunch& w, int tile, int stride)
 {
     std::vector<uint4> v;
     const int s = w.phase / 2;
+    if (!(w.phase & 1)) tile *= bm_groups_per_warp(w.cls);
     long long n = 0;
     for (size_t slot = 0; slot < w.clips.size(); slot++) {
         const int c = w.clips[slot];
@@ -289,9 +293,14 @@ int upload_phase(vbm3d_batch& b, int phase, int tile, int stride, cudaStream_t s
     return VBM3D_OK;
 }
 
+// Block matching: a reference per half warp for one-channel classes (even
+// class numbers), per warp otherwise (batch_bm_kernel's G).
+int bm_groups_per_warp(int cls) { return (cls & 1) ? 1 : 2; }
+
 size_t launch_smem(const WorkLaunch& w, int warps)
 {
-    return (w.phase & 1) ? (size_t)(kViewFloats + warps * w.ws) * sizeof(float) : (size_t)warps * w.ws;
+    return (w.phase & 1) ? (size_t)(kViewFloats + warps * w.ws) * sizeof(float)
+                         : (size_t)warps * bm_groups_per_warp(w.cls) * w.ws;
 }
 
 // Grid of a launch: resident blocks per SM x SMs.

@@ -48,15 +48,18 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // 128 registers and spills (+25 % to +40 %), so k = 7 reads the tables from
 // the shared-memory copy.
 
-template <int STEP, int K, int C>
+// A reference patch takes a group of G lanes, as in bm2_kernel: a warp for
+// three channels, a half warp for one.
+template <int STEP, int K, int C, int G>
 __global__ void __maxnreg__(C == 3 ? 96 : 80)  // as bm2_kernel
 batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
                 unsigned* __restrict__ head, int warp_bytes, const __grid_constant__ BmTable T)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint4 s_item[2];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    unsigned char* ws = smem + (size_t)wid * warp_bytes;
+    const int lane = threadIdx.x & 31, gid = threadIdx.x / G, ngroups = blockDim.x / G;
+    unsigned char* ws = smem + (size_t)gid * warp_bytes;
+    const Grp<G> g(lane);
     claim_item(items, nitems, head, &s_item[0]);
     __syncthreads();
     for (int buf = 0;; buf ^= 1) {
@@ -64,10 +67,10 @@ batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ i
         if (I.x == kNoItem) break;
         claim_item(items, nitems, head, &s_item[buf ^ 1]);
         const int t = (int)I.w;
-        for (unsigned j = wid; j < I.z; j += nwarps) {
-            bm2_ref<K, C>(T.h[t], T.L[t], (long long)I.y + j, ws, lane, T.vid[t], T.fflow[t], T.bflow[t],
-                          T.tab_idx[t], nullptr, nullptr, T.tab_nsx[t]);
-            __syncwarp();
+        for (unsigned j = gid; j < I.z; j += ngroups) {
+            bm2_ref<K, C, G>(T.h[t], T.L[t], (long long)I.y + j, ws, g, T.vid[t], T.fflow[t], T.bflow[t],
+                             T.tab_idx[t], nullptr, nullptr, T.tab_nsx[t]);
+            g.sync();
         }
         __syncthreads();  // publishes the next item
     }

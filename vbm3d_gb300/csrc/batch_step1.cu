@@ -9,10 +9,10 @@ const void* work_kernel_step1(int phase, int cls)
 {
     if (phase == 0) {
         switch (cls) {
-            case 0: return reinterpret_cast<const void*>(batch_bm_kernel<1, 7, 1>);
-            case 1: return reinterpret_cast<const void*>(batch_bm_kernel<1, 7, 3>);
-            case 2: return reinterpret_cast<const void*>(batch_bm_kernel<1, 8, 1>);
-            case 3: return reinterpret_cast<const void*>(batch_bm_kernel<1, 8, 3>);
+            case 0: return reinterpret_cast<const void*>(batch_bm_kernel<1, 7, 1, 16>);
+            case 1: return reinterpret_cast<const void*>(batch_bm_kernel<1, 7, 3, 32>);
+            case 2: return reinterpret_cast<const void*>(batch_bm_kernel<1, 8, 1, 16>);
+            case 3: return reinterpret_cast<const void*>(batch_bm_kernel<1, 8, 3, 32>);
             default: return nullptr;
         }
     }

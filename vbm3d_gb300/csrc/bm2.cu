@@ -25,19 +25,27 @@ namespace {
 
 // Register budget: 96 for three channels (shared memory limits residency
 // to 5 blocks of 4 warps, so 96 registers cost no occupancy and remove
-// spills), 80 for one channel (more resident blocks pay more).
+// spills), 80 for one channel (more resident blocks pay more).  A
+// reference patch takes a group of G lanes: a warp for three channels, a
+// half warp for one (whose distance sums are short, so the per-reference
+// bookkeeping a group runs once is shared by two references per warp).
+template <int K, int C>
+__host__ __device__ constexpr int bm2_group() { return C == 1 ? 16 : 32; }
+
 template <int K, int C>
 __global__ void __maxnreg__(C == 3 ? 96 : 80)
 bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __restrict__ fflow,
            const float* __restrict__ bflow, unsigned* __restrict__ out_idx, float* __restrict__ out_dist,
            unsigned* __restrict__ out_nsimp, unsigned* __restrict__ out_nsx, const Layout L)
 {
+    constexpr int G = bm2_group<K, C>();
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
-    if (r >= P.nrefs) return;
-    bm2_ref<K, C>(P, L, r, smem + (size_t)wid * L.warp_bytes, lane, vid, fflow, bflow, out_idx, out_dist, out_nsimp,
-                  out_nsx);
+    const int lane = threadIdx.x & 31, gid = threadIdx.x / G;
+    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x / G) + gid;
+    if (r >= P.nrefs) return;  // the group's lanes only: the other half of the warp may go on
+    const Grp<G> g(lane);
+    bm2_ref<K, C, G>(P, L, r, smem + (size_t)gid * L.warp_bytes, g, vid, fflow, bflow, out_idx, out_dist,
+                     out_nsimp, out_nsx);
 }
 
 }  // namespace
@@ -51,11 +59,12 @@ cudaError_t launch_bm2(const StepParams& P, const float* vid, const float* fflow
     const Layout L = bm2_layout(P);
     if (!L.warp_bytes) return cudaErrorInvalidValue;
     const int warps = 4;
-    const size_t smem = (size_t)warps * L.warp_bytes;
-    const long long blocks = (count + warps - 1) / warps;
     cudaError_t e = cudaSuccess;
 #define VBM3D_BM2(KV, CV)                                                                                  \
     if (P.k == KV && P.C == CV) {                                                                          \
+        const int groups = warps * 32 / bm2_group<KV, CV>();                                               \
+        const size_t smem = (size_t)groups * L.warp_bytes;                                                 \
+        const long long blocks = (count + groups - 1) / groups;                                            \
         e = cudaFuncSetAttribute(bm2_kernel<KV, CV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
         if (e != cudaSuccess) return e;                                                                    \
         bm2_kernel<KV, CV><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, vid, fflow, bflow, out_idx,   \

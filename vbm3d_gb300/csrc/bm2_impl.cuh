@@ -108,6 +108,47 @@ __host__ __device__ __forceinline__ int bm2_ref_row(int k) { return (k + 1) & ~1
 // Number of positions of a window.
 __device__ __forceinline__ int npos(const PWin& w) { return w.ww * w.wh; }
 
+// The lanes one reference's block matching runs on: the whole warp
+// (G == 32) or one half of it (G == 16, two references per warp).  Every
+// collective goes through these members, over the group's lanes only, so
+// the two halves of a warp may take different branches (a tie, a shorter
+// pass) without waiting for each other.
+template <int G>
+struct Grp {
+    static_assert(G == 16 || G == 32, "a warp or a half warp");
+    int gl;         // lane within the group
+    unsigned mask;  // the group's lanes
+    int base;       // its first lane in the warp
+    __device__ __forceinline__ explicit Grp(int lane)
+        : gl(lane & (G - 1)), mask(G == 32 ? kFull : 0xffffu << (lane & 16)), base(G == 32 ? 0 : (lane & 16))
+    {
+    }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ unsigned ballot(bool p) const
+    {
+        return G == 32 ? __ballot_sync(kFull, p) : (__ballot_sync(mask, p) >> base) & 0xffffu;
+    }
+    __device__ __forceinline__ bool all(bool p) const { return __all_sync(mask, p); }
+    __device__ __forceinline__ unsigned sum(unsigned v) const { return __reduce_add_sync(mask, v); }
+    __device__ __forceinline__ int sum(int v) const { return __reduce_add_sync(mask, v); }
+    __device__ __forceinline__ unsigned minu(unsigned v) const { return __reduce_min_sync(mask, v); }
+    template <class T>
+    __device__ __forceinline__ T shfl(T v, int src) const
+    {
+        return __shfl_sync(mask, v, src, G);
+    }
+    template <class T>
+    __device__ __forceinline__ T shfl_xor(T v, int m) const
+    {
+        return __shfl_xor_sync(mask, v, m, G);
+    }
+    template <class T>
+    __device__ __forceinline__ T shfl_up(T v, int d) const
+    {
+        return __shfl_up_sync(mask, v, d, G);
+    }
+};
+
 // The m smallest valid entries of res[0..n) (scan order), sorted into
 // out[0..m) by the restatement of the reference's partial_sort on one
 // thread: the order among equal distances that std::partial_sort leaves.
@@ -119,10 +160,11 @@ __device__ void tie_sort(const Pair* res, int n, int m, Pair* out, Pair* scratch
     partial_sort(scratch, m, k);
     for (int r = 0; r < m; r++) out[r] = scratch[r];
 }
-__device__ void tie_fallback(const Pair* res, int n, int m, int lane, Pair* out, Pair* scratch)
+template <int G>
+__device__ void tie_fallback(const Pair* res, int n, int m, const Grp<G>& g, Pair* out, Pair* scratch)
 {
-    __syncwarp();
-    if (lane == 0) tie_sort(res, n, m, out, scratch);
+    g.sync();
+    if (g.gl == 0) tie_sort(res, n, m, out, scratch);
 }
 
 constexpr unsigned kNoKey = 0xffffffffu;   // no entry: above every key
@@ -147,53 +189,65 @@ __device__ __forceinline__ float key_dist(unsigned k)
 // Top-min(Nb, #valid) of window w (distances in S.res[w.res ...], scan
 // order), appended sorted to out[*nout]: localSearch's partial_sort
 // (src/vbm3d.cpp:1075-1079).
-__device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, int lane, Pair* out, int& nout,
-                              Pair* scratch)
+template <int G>
+__device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, const Grp<G>& g, Pair* out,
+                              int& nout, Pair* scratch)
 {
     const int n = npos(w);
     const Pair* res = S.res + w.res;
     if (n <= 64) {
-        // up to two entries per lane, as keys: each rank is one warp
+        // up to 64 / G entries per lane, as keys: each rank is one group
         // minimum, and a rank held by two entries is a tie.  Every valid
         // entry counts towards m and has a key below kNoKey, so each of
         // the m ranks finds one; a NaN at a rank goes to the restatement
         // of partial_sort, as a tie does
-        unsigned k0 = kNoKey, k1 = kNoKey, i0 = 0, i1 = 0;
-        if (lane < n) {
-            const Pair e = res[lane];
-            if (e.i != kNone) k0 = dist_key(e.d), i0 = e.i;
+        constexpr int E = 64 / G;
+        unsigned k[E], ix[E];
+        unsigned mine = 0;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int j = g.gl + G * e;
+            k[e] = kNoKey;
+            ix[e] = 0;
+            if (j < n) {
+                const Pair q = res[j];
+                if (q.i != kNone) {
+                    k[e] = dist_key(q.d);
+                    ix[e] = q.i;
+                    mine++;
+                }
+            }
         }
-        if (lane + 32 < n) {
-            const Pair e = res[lane + 32];
-            if (e.i != kNone) k1 = dist_key(e.d), i1 = e.i;
-        }
-        const unsigned mine = (k0 != kNoKey ? 1u : 0u) + (k1 != kNoKey ? 1u : 0u);
-        const int m = min(P.Nb, (int)__reduce_add_sync(kFull, mine));
+        const int m = min(P.Nb, (int)g.sum(mine));
         bool tie = false;
         for (int r = 0; r < m; r++) {
-            const unsigned wmin = __reduce_min_sync(kFull, min(k0, k1));
-            const unsigned c = (k0 == wmin ? 1u : 0u) + (k1 == wmin ? 1u : 0u);
-            if (wmin == kNanKey || __reduce_add_sync(kFull, c) != 1u) {
+            unsigned lm = k[0];
+#pragma unroll
+            for (int e = 1; e < E; e++) lm = min(lm, k[e]);
+            const unsigned wmin = g.minu(lm);
+            unsigned c = 0;
+#pragma unroll
+            for (int e = 0; e < E; e++) c += k[e] == wmin ? 1u : 0u;
+            if (wmin == kNanKey || g.sum(c) != 1u) {
                 tie = true;
                 break;
             }
-            if (k0 == wmin) {
-                out[nout + r] = Pair{key_dist(wmin), i0};
-                k0 = kNoKey;
-            } else if (k1 == wmin) {
-                out[nout + r] = Pair{key_dist(wmin), i1};
-                k1 = kNoKey;
-            }
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (k[e] == wmin) {
+                    out[nout + r] = Pair{key_dist(wmin), ix[e]};
+                    k[e] = kNoKey;
+                }
         }
-        if (tie) tie_fallback(res, n, m, lane, out + nout, scratch);
+        if (tie) tie_fallback(res, n, m, g, out + nout, scratch);
         nout += m;
-        __syncwarp();
+        g.sync();
         return;
     }
     int nvalid = 0;
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        const int j = j0 + lane;
-        nvalid += __popc(__ballot_sync(kFull, j < n && res[j].i != kNone));
+    for (int j0 = 0; j0 < n; j0 += G) {
+        const int j = j0 + g.gl;
+        nvalid += __popc(g.ballot(j < n && res[j].i != kNone));
     }
     const int m = min(P.Nb, nvalid);
     bool tie = false;
@@ -203,7 +257,7 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
         // smallest distance strictly above `last`
         float lmin = __int_as_float(0x7f800000);
         int lj = -1, lcnt = 0;
-        for (int j = lane; j < n; j += 32) {
+        for (int j = g.gl; j < n; j += G) {
             const Pair e = res[j];
             if (e.i == kNone || !(e.d > last)) continue;
             if (lj < 0 || e.d < lmin) {
@@ -216,71 +270,84 @@ __device__ void select_window(const StepHead& P, const Smem& S, const PWin& w, i
         }
         float wmin = lmin;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) wmin = fminf(wmin, __shfl_xor_sync(kFull, wmin, off));
+        for (int off = G / 2; off > 0; off >>= 1) wmin = fminf(wmin, g.shfl_xor(wmin, off));
         const int c = (lj >= 0 && lmin == wmin) ? lcnt : 0;
-        const int tot = __reduce_add_sync(kFull, c);
+        const int tot = g.sum(c);
         if (tot != 1) {
             tie = true;
             break;
         }
-        const unsigned bal = __ballot_sync(kFull, c == 1);
+        const unsigned bal = g.ballot(c == 1);
         const int wl = __ffs(bal) - 1;
-        const int wj = __shfl_sync(kFull, lj, wl);
-        if (lane == 0) out[nout + r] = res[wj];
+        const int wj = g.shfl(lj, wl);
+        if (g.gl == 0) out[nout + r] = res[wj];
         last = wmin;
     }
-    if (tie) tie_fallback(res, n, m, lane, out + nout, scratch);
+    if (tie) tie_fallback(res, n, m, g, out + nout, scratch);
     nout += m;
-    __syncwarp();
+    g.sync();
 }
 
 // Sorted smallest `m` of a[0..n) written to out (std::partial_sort order):
-// exact ranks when all keys of the prefix are distinct, else the
-// restatement of the reference's routine on one lane.
-__device__ void small_partial_sort(Pair* a, int m, int n, int lane)
+// exact ranks (EP entries per lane, EP = 1 for a warp, 2 for a half warp)
+// when all keys of the prefix are distinct, else the restatement of the
+// reference's routine on one lane.
+template <int G>
+__device__ void small_partial_sort(Pair* a, int m, int n, const Grp<G>& g)
 {
-    if (n > 32) {
-        if (lane == 0) partial_sort(a, m, n);
-        __syncwarp();
+    constexpr int EP = G == 32 ? 1 : 2;
+    if (n > EP * G) {
+        if (g.gl == 0) partial_sort(a, m, n);
+        g.sync();
         return;
     }
     bool ok = true;
-    int rank = 0;
-    Pair mine = {0.f, 0};
-    if (lane < n) {
-        mine = a[lane];
-        for (int j = 0; j < n; j++) {
-            const float d = a[j].d;
-            if (d < mine.d) rank++;
-            else if (d == mine.d && j != lane) ok = false;
+    int rank[EP];
+    Pair mine[EP];
+#pragma unroll
+    for (int e = 0; e < EP; e++) {
+        const int j = g.gl + G * e;
+        rank[e] = 0;
+        mine[e] = Pair{0.f, 0};
+        if (j < n) {
+            mine[e] = a[j];
+            for (int i = 0; i < n; i++) {
+                const float d = a[i].d;
+                if (d < mine[e].d) rank[e]++;
+                else if (d == mine[e].d && i != j) ok = false;
+            }
         }
     }
     // ties among entries that cannot reach the prefix do not matter, but
     // keep it simple: any tie sends the list to the exact routine
-    ok = __all_sync(kFull, ok);
-    __syncwarp();
+    ok = g.all(ok);
+    g.sync();
     if (ok) {
-        if (lane < n && rank < m) a[rank] = mine;  // ranks are distinct: a permutation of the prefix
-    } else if (lane == 0) {
+#pragma unroll
+        for (int e = 0; e < EP; e++)
+            if (g.gl + G * e < n && rank[e] < m) a[rank[e]] = mine[e];  // distinct ranks: a permutation of the prefix
+    } else if (g.gl == 0) {
         partial_sort(a, m, n);
     }
-    __syncwarp();
+    g.sync();
 }
 
-// select_window for every window of a phase at once (nw <= 32 / G, each
-// window at most 32 positions): window w on the G lanes of group w, up to
-// 32 / G entries per lane, each rank one group minimum of the keys and one
-// group count of the entries holding it.  The picks of the windows of a
-// chain are appended in window order to the chain's frame candidates
-// (S.fc: forward chain first), as the per-window calls append them; nfc_f
-// and nfc_b count them.  Windows with a tie (or a NaN) at a rank go, one
-// at a time, to the partial_sort restatement on their group's first lane.
-template <int G>
-__device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, int lane, int& nfc_f, int& nfc_b)
+// select_window for every window of a phase at once (nw <= G / GS, each
+// window at most 32 positions): window w on the GS lanes of subgroup w of
+// the group, up to 32 / GS entries per lane, each rank one subgroup minimum
+// of the keys and one subgroup count of the entries holding it.  The picks
+// of the windows of a chain are appended in window order to the chain's
+// frame candidates (S.fc: forward chain first), as the per-window calls
+// append them; nfc_f and nfc_b count them.  Windows with a tie (or a NaN)
+// at a rank go, one at a time, to the partial_sort restatement on their
+// subgroup's first lane.
+template <int GS, int G>
+__device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, const Grp<G>& g, int& nfc_f,
+                             int& nfc_b)
 {
-    constexpr int E = 32 / G;
+    constexpr int E = 32 / GS, NS = G / GS;
     const int Nb = P.Nb;
-    const int w = lane / G, gl = lane & (G - 1);
+    const int w = g.gl / GS, sl = g.gl & (GS - 1);
     int n = 0, res = 0;
     if (w < nw) {
         const PWin& W = S.pw[w];
@@ -291,7 +358,7 @@ __device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, 
     unsigned nv = 0;
 #pragma unroll
     for (int i = 0; i < E; i++) {
-        const int j = gl + G * i;
+        const int j = sl + GS * i;
         key[i] = kNoKey;
         idx[i] = 0;
         if (j < n) {
@@ -304,16 +371,16 @@ __device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, 
         }
     }
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) nv += __shfl_xor_sync(kFull, nv, o);
-    const int m = min(Nb, (int)nv);  // 0 for the groups past nw
+    for (int o = GS / 2; o > 0; o >>= 1) nv += g.shfl_xor(nv, o);
+    const int m = min(Nb, (int)nv);  // 0 for the subgroups past nw
     // the window's chain (forward: windows 0 .. Nb-1 when the forward
     // chain is active) and its offset among the chain's candidates
     const bool fwd = fa && w < Nb;
     const int c0 = fwd ? 0 : (fa ? Nb : 0);
     int off = 0, nf = 0, nb = 0;
 #pragma unroll
-    for (int v = 0; v < E; v++) {
-        const int mv = __shfl_sync(kFull, m, v * G);
+    for (int v = 0; v < NS; v++) {
+        const int mv = g.shfl(m, v * GS);
         if (fa && v < Nb) nf += mv;
         else nb += mv;
         if (v >= c0 && v < w) off += mv;
@@ -325,14 +392,14 @@ __device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, 
 #pragma unroll
         for (int i = 1; i < E; i++) gmin = min(gmin, key[i]);
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) gmin = min(gmin, (unsigned)__shfl_xor_sync(kFull, gmin, o));
+        for (int o = GS / 2; o > 0; o >>= 1) gmin = min(gmin, (unsigned)g.shfl_xor(gmin, o));
         unsigned c = 0;
 #pragma unroll
         for (int i = 0; i < E; i++) c += key[i] == gmin ? 1u : 0u;
         unsigned cs = c;
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) cs += __shfl_xor_sync(kFull, cs, o);
-        if (tie || r >= m) continue;  // uniform over the group
+        for (int o = GS / 2; o > 0; o >>= 1) cs += g.shfl_xor(cs, o);
+        if (tie || r >= m) continue;  // uniform over the subgroup
         if (gmin == kNanKey || cs != 1u) {
             tie = true;
             continue;
@@ -344,10 +411,10 @@ __device__ void select_phase(const StepHead& P, const Smem& S, int nw, bool fa, 
                 key[i] = kNoKey;
             }
     }
-    __syncwarp();
-    for (unsigned tb = __ballot_sync(kFull, gl == 0 && tie); tb; tb &= tb - 1) {
-        if (lane == __ffs(tb) - 1) tie_sort(S.res + res, n, m, out, S.scr);
-        __syncwarp();
+    g.sync();
+    for (unsigned tb = g.ballot(sl == 0 && tie); tb; tb &= tb - 1) {
+        if (g.gl == __ffs(tb) - 1) tie_sort(S.res + res, n, m, out, S.scr);
+        g.sync();
     }
     nfc_f = nf;
     nfc_b = nb;
@@ -395,52 +462,52 @@ __device__ __forceinline__ void store_entry(const StepHead& P, const Smem& S, co
 // each window and the K reference pixels once, and the two windows share
 // each packed f32x2 operation.  An odd last window runs in passes of its
 // own, a lane evaluating positions (dy, 2cx) and (dy, 2cx + 1) of it as the
-// packed pair.  Every distance is the reference's sequential sum over
-// (c, hy, hx).  Only the slot (window, dy, dx) is live across the sums; the
-// windows' fields are read again for the results.
-template <int K, int C>
-__device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int lane, int rx, int ry, int rt,
+// packed pair.  A pass covers G slots.  Every distance is the reference's
+// sequential sum over (c, hy, hx).  Only the slot (window, dy, dx) is live
+// across the sums; the windows' fields are read again for the results.
+template <int K, int C, int G>
+__device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const Grp<G>& g, int rx, int ry, int rt,
                                 int pitch, int plane)
 {
     constexpr int KK = K * K, KR = (K + 1) & ~1;  // KR: bm2_ref_row(K)
     const int npairs = nw >> 1;
-    // pair `lane` (lanes < npairs): `cols` slot columns (ceil(max ww / 2)),
+    // pair `gl` (lanes < npairs): `cols` slot columns (ceil(max ww / 2)),
     // max wh rows; pend = one past its last slot (inclusive scan)
     int cols = 1, slots = 0;
-    if (lane < npairs) {
-        const PWin& A = S.pw[2 * lane];
-        const PWin& B = S.pw[2 * lane + 1];
+    if (g.gl < npairs) {
+        const PWin& A = S.pw[2 * g.gl];
+        const PWin& B = S.pw[2 * g.gl + 1];
         cols = (max(A.ww, B.ww) + 1) >> 1;
         slots = max(A.wh, B.wh) * cols;
     }
     int pend = slots;
 #pragma unroll
     for (int o = 1; o < kMaxNb; o <<= 1) {
-        const int v = __shfl_up_sync(kFull, pend, o);
-        if (lane >= o) pend += v;
+        const int v = g.shfl_up(pend, o);
+        if (g.gl >= o) pend += v;
     }
-    const int total = npairs > 0 ? __shfl_sync(kFull, pend, npairs - 1) : 0;
-    const int pair_passes = (total + 31) >> 5;
+    const int total = npairs > 0 ? g.shfl(pend, npairs - 1) : 0;
+    const int pair_passes = (total + G - 1) / G;
     int lone_cols = 1, lone_slots = 0;
     if (nw & 1) {
         const PWin& L = S.pw[nw - 1];
         lone_cols = (L.ww + 1) >> 1;
         lone_slots = L.wh * lone_cols;
     }
-    const int passes = pair_passes + ((lone_slots + 31) >> 5);
+    const int passes = pair_passes + (lone_slots + G - 1) / G;
     const float nz = P.neg_zero;
     const float norm = (float)(KK * C);
 
     for (int pass = 0; pass < passes; pass++) {
-        const bool pm = pass < pair_passes;  // uniform over the warp
-        const int sl = (pm ? pass : pass - pair_passes) * 32 + lane;
+        const bool pm = pass < pair_passes;  // uniform over the group
+        const int sl = (pm ? pass : pass - pair_passes) * G + g.gl;
         // the lane's slot: window wa (pairs: and wa + 1), row dy, column dx
         int wa = nw - 1, j = sl, limit = lone_slots, cp = lone_cols;
         if (pm) {
             int p = 0;
-            for (int q = 0; q + 1 < npairs; q++) p += sl >= __shfl_sync(kFull, pend, q) ? 1 : 0;
-            const int e = __shfl_sync(kFull, pend, p), n = __shfl_sync(kFull, slots, p);
-            cp = __shfl_sync(kFull, cols, p);
+            for (int q = 0; q + 1 < npairs; q++) p += sl >= g.shfl(pend, q) ? 1 : 0;
+            const int e = g.shfl(pend, p), n = g.shfl(slots, p);
+            cp = g.shfl(cols, p);
             wa = 2 * p;
             j = sl - (e - n);
             limit = n;
@@ -516,14 +583,14 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, int la
             }
         }
     }
-    __syncwarp();
+    g.sync();
 }
 
 // Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
-// channels, at tile pitch `pitch`.
-
-template <int K, int C>
-__device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, int lane,
+// channels, at tile pitch `pitch`.  A warp copies two rows of a tile up to
+// 16 wide per step, a half warp one row (16 columns) per step.
+template <int K, int C, int G>
+__device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, const Grp<G>& g,
                             int pitch, int plane)
 {
     // every tile row of every window is copied asynchronously, then waited
@@ -534,8 +601,13 @@ __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __res
     for (int w = 0; w < nw; w++) {
         const PWin pwn = S.pw[w];
         const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
-        const int x = tw <= 16 ? (lane & 15) : lane, ystep = tw <= 16 ? 2 : 1, y0 = tw <= 16 ? (lane >> 4) : 0;
-        if (x < tw) {
+        int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
+        if (G == 32 && tw <= 16) {
+            x0 = g.gl & 15;
+            ystep = 2;
+            y0 = g.gl >> 4;
+        }
+        for (int x = x0; x < tw; x += xstep) {
             const float* src = vid + pwn.t * whc + (pwn.y0 + y0) * W + pwn.x0 + x;
             const unsigned dst = tiles + 4u * (unsigned)(pwn.tile + y0 * pitch + x);
             const long long sstep = ystep * W;
@@ -547,24 +619,26 @@ __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __res
 #pragma unroll 4
                 for (int y = y0; y < th; y += ystep, s += sstep, d += dstep) cp_async4s(d, s);
             }
+            if (G == 32 && tw <= 16) break;  // the two half warps cover the 16 columns
         }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncwarp();
+    g.sync();
 }
 
 // Registers the phase's windows in the list of scanned windows (after the
 // phase's seen masks were computed against the earlier ones).
-__device__ void register_windows(const Smem& S, int nw, int lane)
+template <int G>
+__device__ void register_windows(const Smem& S, int nw, const Grp<G>& g)
 {
     const int n0 = S.cnt[2];
-    if (lane < nw) {
-        const PWin pwn = S.pw[lane];
-        S.wins[n0 + lane] = Win{pwn.t, pwn.x0, pwn.x0 + pwn.ww - 1, pwn.y0, pwn.y0 + pwn.wh - 1};
+    if (g.gl < nw) {
+        const PWin pwn = S.pw[g.gl];
+        S.wins[n0 + g.gl] = Win{pwn.t, pwn.x0, pwn.x0 + pwn.ww - 1, pwn.y0, pwn.y0 + pwn.wh - 1};
     }
-    __syncwarp();
-    if (lane == 0) S.cnt[2] = n0 + nw;
-    __syncwarp();
+    g.sync();
+    if (g.gl == 0) S.cnt[2] = n0 + nw;
+    g.sync();
 }
 
 // The clamped window of side s around (cx, cy) (src/vbm3d.cpp:1045-1053).
@@ -587,17 +661,18 @@ __device__ __forceinline__ PWin make_window(const StepHead& P, int t, int cx, in
     return w;
 }
 
-// Block matching of reference patch r by one warp (lane 0..31), with the
-// warp's shared-memory region ws laid out by L.
-template <int K, int C>
-__device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long long r, unsigned char* ws, int lane,
-                                        const float* __restrict__ vid, const float* __restrict__ fflow,
-                                        const float* __restrict__ bflow, unsigned* __restrict__ out_idx,
-                                        float* __restrict__ out_dist, unsigned* __restrict__ out_nsimp,
-                                        unsigned* __restrict__ out_nsx)
+// Block matching of reference patch r by the G lanes of group g (a warp,
+// or half of one), with the group's shared-memory region ws laid out by L.
+template <int K, int C, int G>
+__device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long long r, unsigned char* ws,
+                                        const Grp<G>& g, const float* __restrict__ vid,
+                                        const float* __restrict__ fflow, const float* __restrict__ bflow,
+                                        unsigned* __restrict__ out_idx, float* __restrict__ out_dist,
+                                        unsigned* __restrict__ out_nsimp, unsigned* __restrict__ out_nsx)
 {
     constexpr int KK = K * K;
     const int Nb = P.Nb;
+    const int gl = g.gl;
     Smem S;
     size_t off = 0;
     S.refp = reinterpret_cast<float2*>(ws + off);
@@ -622,37 +697,37 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
 
     int rx, ry, rt;
     ref_coords(P, r, rx, ry, rt);
-    for (int e = lane; e < C * KK; e += 32) {
+    for (int e = gl; e < C * KK; e += G) {
         const int c = e / KK, pq = e - c * KK, py = pq / K, px = pq - py * K;
         const float v = __ldg(vid + (size_t)rt * P.whc + (size_t)c * P.wh + (size_t)(ry + py) * P.W + rx + px);
         S.refp[(c * K + py) * bm2_ref_row(K) + px] = make_float2(v, v);
     }
-    if (lane == 0) {
+    if (gl == 0) {
         S.cnt[2] = 0;  // windows scanned
     }
-    __syncwarp();
+    g.sync();
 
     // ---- phase 0: the reference frame (src/vbm3d.cpp:1114-1119)
     {
         const int pitch = bm2_pitch(P.Ns, K), plane = pitch * (P.Ns + K - 1);
-        if (lane == 0) {
+        if (gl == 0) {
             PWin w = make_window(P, rt, rx, ry, P.Ns, 0);
             S.pw[0] = w;
             S.cnt[3] = 0;
         }
-        __syncwarp();
-        stage_tiles<K, C>(P, S, vid, 1, lane, pitch, plane);
-        phase_distances<K, C>(P, S, 1, lane, rx, ry, rt, pitch, plane);
-        register_windows(S, 1, lane);
+        g.sync();
+        stage_tiles<K, C>(P, S, vid, 1, g, pitch, plane);
+        phase_distances<K, C>(P, S, 1, g, rx, ry, rt, pitch, plane);
+        register_windows(S, 1, g);
         int n0 = 0;
-        select_window(P, S, S.pw[0], lane, S.best, n0, S.scr);
-        if (lane < Nb) {
+        select_window(P, S, S.pw[0], g, S.best, n0, S.scr);
+        if (gl < Nb) {
             // the reference reads Nb entries here (src/vbm3d.cpp:1115-1119);
             // the host rejects grids whose corner window holds fewer
-            S.cen[lane] = S.best[lane].i;          // forward chain centres
-            S.cen[kMaxNb + lane] = S.best[lane].i; // backward chain centres
+            S.cen[gl] = S.best[gl].i;          // forward chain centres
+            S.cen[kMaxNb + gl] = S.best[gl].i; // backward chain centres
         }
-        __syncwarp();
+        g.sync();
     }
 
     const int fend = min(rt + P.Nf, P.F - P.kt) - rt;
@@ -664,16 +739,16 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
     const int pitch = bm2_pitch(P.Npr, K), plane = pitch * (P.Npr + K - 1);
     const int tile_sz = C * plane;
     for (int f = 1; f <= nphase; f++) {
-        // windows of this phase, one per lane: forward step f
-        // (src/vbm3d.cpp:1126-1133), then backward step f (:1150-1157)
+        // windows of this phase, one per lane (nw <= 2 kMaxNb <= G): forward
+        // step f (src/vbm3d.cpp:1126-1133), then backward step f (:1150-1157)
         const bool fa = f <= fend, ba = f <= bend;
         const int nw = (fa ? Nb : 0) + (ba ? Nb : 0);
         {
             PWin w;
             int n = 0;
-            if (lane < nw) {
-                const int chain = (fa && lane < Nb) ? 1 : 2;
-                const int m = chain == 1 ? lane : lane - (fa ? Nb : 0);
+            if (gl < nw) {
+                const int chain = (fa && gl < Nb) ? 1 : 2;
+                const int m = chain == 1 ? gl : gl - (fa ? Nb : 0);
                 int px, py, pt;
                 unpack_xyt(S.cen[(chain - 1) * kMaxNb + m], rt, px, py, pt);
                 const float* flow = chain == 1 ? fflow : bflow;
@@ -684,49 +759,54 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
                 const float fy = fl ? __ldg(fl + P.wh + (size_t)(py + K / 2) * P.W + px + K / 2) : 0.f;
                 py = min(max((int)((float)py + roundf(fy)), 0), P.H - K);
                 w = make_window(P, chain == 1 ? pt + 1 : pt - 1, px, py, P.Npr, chain);
-                w.tile = bm2_tile_offset(lane, tile_sz);
+                w.tile = bm2_tile_offset(gl, tile_sz);
                 n = npos(w);
             }
             // exclusive prefix sum of the window sizes: result offsets
             int incl = n;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += v;
+            for (int o = 1; o < G; o <<= 1) {
+                const int v = g.shfl_up(incl, o);
+                if (gl >= o) incl += v;
             }
-            if (lane < nw) {
+            if (gl < nw) {
                 w.res = incl - n;
-                S.pw[lane] = w;
-                S.cnt[3 + lane] = S.cnt[2] + lane;  // earlier windows: all registered + earlier in this phase
+                S.pw[gl] = w;
+                S.cnt[3 + gl] = S.cnt[2] + gl;  // earlier windows: all registered + earlier in this phase
             }
-            __syncwarp();
+            g.sync();
         }
         // this phase's windows must be visible to the seen test of later
         // windows of the same phase: register them first, then test each
         // window against the windows registered before it (S.cnt[3 + w])
-        register_windows(S, nw, lane);
-        // seen masks: windows registered before each one, on its frame
+        register_windows(S, nw, g);
+        // seen masks: windows registered before each one, on its frame (up
+        // to 64 windows, G per ballot)
         for (int w = 0; w < nw; w++) {
             const int lim = S.cnt[3 + w], wt = S.pw[w].t;
-            const unsigned lo = __ballot_sync(kFull, lane < lim && S.wins[lane].t == wt);
-            const unsigned hi = __ballot_sync(kFull, lane + 32 < lim && S.wins[lane + 32].t == wt);
-            if (lane == 0) S.pw[w].seen = ((unsigned long long)hi << 32) | lo;
+            unsigned long long bits = 0ull;
+#pragma unroll
+            for (int c = 0; c < 64 / G; c++) {
+                const int wi = gl + G * c;
+                bits |= (unsigned long long)g.ballot(wi < lim && S.wins[wi].t == wt) << (G * c);
+            }
+            if (gl == 0) S.pw[w].seen = bits;
         }
-        __syncwarp();
-        stage_tiles<K, C>(P, S, vid, nw, lane, pitch, plane);
-        phase_distances<K, C>(P, S, nw, lane, rx, ry, rt, pitch, plane);
+        g.sync();
+        stage_tiles<K, C>(P, S, vid, nw, g, pitch, plane);
+        phase_distances<K, C>(P, S, nw, g, rx, ry, rt, pitch, plane);
 
         // per chain: top-Nb of each window, then of their union
         int nfc2[2] = {0, 0};
         if (nw <= 4 && P.Npr * P.Npr <= 32) {
-            if (nw <= 2) select_phase<16>(P, S, nw, fa, lane, nfc2[0], nfc2[1]);
-            else select_phase<8>(P, S, nw, fa, lane, nfc2[0], nfc2[1]);
+            if (nw <= 2) select_phase<G / 2>(P, S, nw, fa, g, nfc2[0], nfc2[1]);
+            else select_phase<G / 4>(P, S, nw, fa, g, nfc2[0], nfc2[1]);
         } else {
             int w0 = 0;
             for (int chain = 1; chain <= 2; chain++) {
                 if ((chain == 1 && f > fend) || (chain == 2 && f > bend)) continue;
                 for (int m = 0; m < Nb; m++)
-                    select_window(P, S, S.pw[w0 + m], lane, S.fc + (chain - 1) * Nb * Nb, nfc2[chain - 1], S.scr);
+                    select_window(P, S, S.pw[w0 + m], g, S.fc + (chain - 1) * Nb * Nb, nfc2[chain - 1], S.scr);
                 w0 += Nb;
             }
         }
@@ -735,15 +815,15 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
             Pair* fc = S.fc + (chain - 1) * Nb * Nb;
             const int nfc = nfc2[chain - 1];
             const int m2 = min(Nb, nfc);
-            small_partial_sort(fc, m2, nfc, lane);
+            small_partial_sort(fc, m2, nfc, g);
             Pair* dst = chain == 1 ? bestf + nbf : bestb + nbb;
-            if (lane < m2) {
-                S.cen[(chain - 1) * kMaxNb + lane] = fc[lane].i;
-                dst[lane] = fc[lane];
+            if (gl < m2) {
+                S.cen[(chain - 1) * kMaxNb + gl] = fc[gl].i;
+                dst[gl] = fc[gl];
             }
             if (chain == 1) nbf += m2;
             else nbb += m2;
-            __syncwarp();
+            g.sync();
         }
     }
 
@@ -752,29 +832,27 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
     Pair* lst = S.res;
     const int nb0 = Nb;  // frame-t picks: exactly Nb (the host validates the corner window)
     const int nbest = nb0 + nbf + nbb;
-    for (int j = lane; j < nbest; j += 32) {
+    for (int j = gl; j < nbest; j += G) {
         Pair e;
         if (j < nb0) e = S.best[j];
         else if (j < nb0 + nbf) e = bestf[j - nb0];
         else e = bestb[j - nb0 - nbf];
         lst[j] = e;
     }
-    __syncwarp();
+    g.sync();
     const int nsimp = min(P.N, nbest);
-    if (nbest <= 32) small_partial_sort(lst, nsimp, nbest, lane);
-    else if (lane == 0) partial_sort(lst, nsimp, nbest);
-    __syncwarp();
-    if (lane < P.N) {
+    small_partial_sort(lst, nsimp, nbest, g);
+    for (int j = gl; j < P.N; j += G) {
         unsigned oi = kNone;
-        if (lane < nsimp) {
+        if (j < nsimp) {
             int x, y, t;
-            unpack_xyt(lst[lane].i, rt, x, y, t);
+            unpack_xyt(lst[j].i, rt, x, y, t);
             oi = patch_index(P, x, y, t);
         }
-        out_idx[(size_t)r * P.N + lane] = oi;
-        if (out_dist) out_dist[(size_t)r * P.N + lane] = lane < nsimp ? lst[lane].d : 0.f;
+        out_idx[(size_t)r * P.N + j] = oi;
+        if (out_dist) out_dist[(size_t)r * P.N + j] = j < nsimp ? lst[j].d : 0.f;
     }
-    if (lane == 0) {
+    if (gl == 0) {
         int thr = nsimp - 1;
         while (lst[thr].d > P.tau && thr > 0) thr--;
         unsigned pw2 = 1;
