@@ -259,7 +259,7 @@ def fp32_peak(dev, clocks):
 
 # DRAM bytes (read + write) per reference patch of the batched step-2 block
 # matching of the RGB k = 7 clips: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3> on the full batch
+# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3, 32> on the full batch
 # (python -m vbm3d_gb300.profile_case --batch 64): 1.449 GB + 0.437 GB for
 # 12 308 991 reference patches.
 BM2_DRAM_BYTES_PER_REF = 153.0
@@ -424,8 +424,9 @@ def run_gpu(args):
         peak, peak_src = fp32_peak(dev, clocks)
         achieved = flops / (bm["ms"] / 1e3) / 1e12
         traffic = BM2_DRAM_BYTES_PER_REF * bm["refs"] if (step, bm["k"], bm["channels"]) == (2, 7, 3) else None
-        roofline = {"kernel": "batch_bm_kernel<%d, %d, %d> (step-%d block matching, %d clips)"
-                              % (step, bm["k"], bm["channels"], step, bm["clips"]),
+        roofline = {"kernel": "batch_bm_kernel<%d, %d, %d, %d> (step-%d block matching, %d clips)"
+                              % (step, bm["k"], bm["channels"], 16 if bm["channels"] == 1 else 32, step,
+                                 bm["clips"]),
                     "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic,
                     "traffic_source": "ncu DRAM bytes (read + write) of this kernel on the full batch, per "

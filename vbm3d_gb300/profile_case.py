@@ -28,7 +28,7 @@ import torch
 import vbm3d_gb300 as vb
 from vbm3d_gb300.synth import batch_specs, make_clip
 
-FIXED = dict(bm1_tile=4, bm1_warps=4, filter1_tile=16, filter1_warps=8, bm2_tile=8, bm2_warps=4, filter2_tile=16,
+FIXED = dict(bm1_tile=4, bm1_warps=4, filter1_tile=32, filter1_warps=8, bm2_tile=4, bm2_warps=4, filter2_tile=32,
              filter2_warps=8, no_graph=1)
 
 
