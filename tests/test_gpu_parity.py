@@ -135,6 +135,19 @@ def test_block_matching_ties(dev, oracle):
     assert_bm_equal(gpu_similar(flat, p, dev), oracle.similar(p, flat), p)
 
 
+@pytest.mark.parametrize("channels", [1, 3])
+def test_block_matching_wide_windows(dev, oracle, channels):
+    # Ns = 11: frame-t tiles 17 (k = 7) or 18 (k = 8) columns wide, staged
+    # in column steps (a half warp per reference for one channel, a warp
+    # for three); Npr = 9: forward / backward windows of 81 positions,
+    # selected one window at a time
+    rng = np.random.default_rng(11 + channels)
+    vid = rng.normal(120, 30, (6, channels, 44, 52)).astype(np.float32)
+    for step in (1, 2):
+        p = oracle.default_params(step, 20.0).replace(Ns=11, Npr=9)
+        assert_bm_equal(gpu_similar(vid, p, dev), oracle.similar(p, vid), p)
+
+
 def ratio(num, den, fb):
     return np.where(den == 0, fb, num / np.where(den == 0, 1, den)).astype(np.float32)
 
