@@ -175,3 +175,23 @@ def test_profile_run_matches_graph_run(dev, clips):
         assert refs == want
     assert all(l["ms"] > 0 and l["items"] > 0 and l["grid"] > 0 for l in launches)
     b.close()
+
+
+def test_wide_search_windows(dev):
+    # per-clip parameters with Ns = 11 and Npr = 9: frame-t tiles wider than
+    # 16 columns and forward / backward windows of 81 positions, in the
+    # batched block matching of one channel (half warps) and three (warps)
+    specs = []
+    for i, (w, h, f, c, s) in enumerate([(56, 44, 6, 1, 20.0), (60, 40, 6, 3, 40.0)]):
+        clean, noisy, _, _ = make_clip(w, h, f, c, s, 4200 + i)
+        p1 = vb.default_params(1, s).replace(Ns=11, Npr=9)
+        p2 = vb.default_params(2, s).replace(Ns=11, Npr=9)
+        specs.append(dict(clean=clean, noisy=noisy, sigma=s, p1=p1, p2=p2))
+    b = vb.Batch([dict(noisy=gpu(c["noisy"], dev), sigma=c["sigma"], p1=c["p1"], p2=c["p2"]) for c in specs],
+                 color_space=True)
+    basic, den = b.run()
+    torch.cuda.synchronize()
+    for i, c in enumerate(specs):
+        pb, pd = vb.run(gpu(c["noisy"], dev), c["sigma"], c["p1"], c["p2"], color_space=True)
+        assert_close(c["clean"], basic[i].cpu().numpy(), den[i].cpu().numpy(), pb.cpu().numpy(), pd.cpu().numpy())
+    b.close()
