@@ -24,8 +24,11 @@ Multi-GPU: the path has no exchange step; --gpus N runs N independent
 replicas (one per rank) and value = total clip frames / max time.
 
 --impl reference times the reference's CPU implementation of the path on
-the host cores instead: the oracle port (oracle/vbm3d_oracle.c) with all
-host threads, each step a bounded sample of the same workload.
+the host cores instead: the oracle port (oracle/vbm3d_oracle.c), each step a
+bounded sample of the same workload.  The CPU figure (that line's value and
+the GPU line's cpu_baseline) is the higher of two modes: all host threads
+on one clip at a time (OpenMP), and independent clips of at most 8 frames
+as concurrent single-threaded processes, one per host thread.
 """
 import argparse
 import json
@@ -117,6 +120,64 @@ def time_cpu(samples, steps=1):
             f, _, h, w = noisy.shape
             mpf += w * h * f / 1e6
     return mpf / (time.perf_counter() - t0), th
+
+
+def _port_warm(_):
+    from oracle.pyoracle import Oracle
+    Oracle()
+    return 0
+
+
+def _port_job(job):
+    """One clip through the oracle port on one thread (a worker process)."""
+    noisy, sigma = job
+    from oracle.pyoracle import Oracle
+    o = Oracle()
+    o.run(sigma, noisy, o.default_params(1, sigma), o.default_params(2, sigma), color_space=COLOR, threads=1)
+    f, _, h, w = noisy.shape
+    return w * h * f / 1e6
+
+
+PROC_CHUNK_F = 8  # process mode: a sample clip runs as independent clips of at most 8 frames
+
+
+def proc_jobs(samples, th):
+    """Jobs of the process mode: each sample clip cut into clips of at most
+    PROC_CHUNK_F frames, repeated until there is a job per worker, largest
+    first; returns (jobs, repeats)."""
+    chunks = [(a[t:t + PROC_CHUNK_F], s) for a, s in samples for t in range(0, a.shape[0], PROC_CHUNK_F)]
+    reps = max(1, -(-th // len(chunks)))
+    return sorted([c for c in chunks for _ in range(reps)], key=lambda c: -c[0].size), reps
+
+
+def time_cpu_procs(samples, steps=1):
+    """The same sample as independent single-threaded runs, one worker
+    process per host thread; returns (Mpix-frames/s, processes, repeats).
+    The workers are spawned (the parent may hold a CUDA context) and have
+    loaded the oracle before the clock starts."""
+    import multiprocessing as mp
+    th = cpu_threads()
+    jobs, reps = proc_jobs(samples, th)
+    with mp.get_context("spawn").Pool(th) as pool:
+        pool.map(_port_warm, range(th), chunksize=1)
+        t0 = time.perf_counter()
+        mpf = sum(pool.map(_port_job, jobs * steps, chunksize=1))
+        dt = time.perf_counter() - t0
+    return mpf / dt, th, reps
+
+
+def cpu_baseline(samples, desc, steps=1):
+    """cpu_baseline of the JSON line: the oracle port on the host cores in
+    two modes, all threads on one clip at a time (OpenMP) and independent
+    clips as concurrent single-threaded processes; value = the higher."""
+    v_omp, th = time_cpu(samples, steps)
+    v_proc, npr, reps = time_cpu_procs(samples, steps)
+    return {"value": round(max(v_omp, v_proc), 4), "unit": UNIT, "cores": th, "kind": "port",
+            "sample": desc + "; the higher of two modes",
+            "modes": {"openmp": {"value": round(v_omp, 4), "threads": th},
+                      "processes": {"value": round(v_proc, 4), "processes": npr,
+                                    "jobs": "the sample in clips of at most %d frames, x %d, one thread each"
+                                            % (PROC_CHUNK_F, reps)}}}
 
 
 def cpu_sample(workload, clips=None, noisy=None):
@@ -227,15 +288,15 @@ def run_reference(args):
         workload = WORKLOAD_1080
     if args.warmup > 0:
         time_cpu([(a[:2], s) for a, s in samples[:2]])
-    value, th = time_cpu(samples, steps=args.steps)
+    cpu = cpu_baseline(samples, desc, steps=args.steps)
+    value = cpu["value"]
     mpf = sum(a.shape[0] * a.shape[2] * a.shape[3] for a, _ in samples) / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "ms_per_step": round(mpf / value * 1e3, 1), "vs_baseline": None, "dtype": "f32", "data": DATA,
         "config": {"workload": workload, "sample": desc},
-        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": th, "kind": "port",
-                         "sample": desc + ", %d OpenMP threads" % th},
+        "cpu_baseline": cpu,
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -531,9 +592,7 @@ def run_gpu(args):
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
             samples, desc = cpu_sample("batch64", clips=clips)
-            val, th = time_cpu(samples)
-            cpu = {"value": round(val, 4), "unit": UNIT, "cores": th, "kind": "port",
-                   "sample": desc + ", %d OpenMP threads" % th}
+            cpu = cpu_baseline(samples, desc)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
@@ -595,9 +654,7 @@ def run_gpu(args):
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
             samples, desc = cpu_sample("1080p30", noisy=noisy)
-            val, th = time_cpu(samples)
-            cpu = {"value": round(val, 4), "unit": UNIT, "cores": th, "kind": "port",
-                   "sample": desc + ", %d OpenMP threads" % th}
+            cpu = cpu_baseline(samples, desc)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
