@@ -28,7 +28,8 @@ the host cores instead: the oracle port (oracle/vbm3d_oracle.c), each step a
 bounded sample of the same workload.  The CPU figure (that line's value and
 the GPU line's cpu_baseline) is the higher of two modes: all host threads
 on one clip at a time (OpenMP), and independent clips of at most 8 frames
-as concurrent single-threaded processes, one per host thread.
+as concurrent single-threaded processes, one per host thread, with at
+least four clips queued per process.
 """
 import argparse
 import json
@@ -138,15 +139,17 @@ def _port_job(job):
     return w * h * f / 1e6
 
 
-PROC_CHUNK_F = 8  # process mode: a sample clip runs as independent clips of at most 8 frames
+PROC_CHUNK_F = 8    # process mode: a sample clip runs as independent clips of at most 8 frames
+PROC_JOBS_PER = 4   # and at least this many jobs per worker, so that the last jobs' tail stays short
 
 
 def proc_jobs(samples, th):
     """Jobs of the process mode: each sample clip cut into clips of at most
-    PROC_CHUNK_F frames, repeated until there is a job per worker, largest
-    first; returns (jobs, repeats)."""
+    PROC_CHUNK_F frames, repeated until there are PROC_JOBS_PER jobs per
+    worker, largest first (a steady stream of clips keeps every core busy,
+    as a serving loop would); returns (jobs, repeats)."""
     chunks = [(a[t:t + PROC_CHUNK_F], s) for a, s in samples for t in range(0, a.shape[0], PROC_CHUNK_F)]
-    reps = max(1, -(-th // len(chunks)))
+    reps = max(1, -(-PROC_JOBS_PER * th // len(chunks)))
     return sorted([c for c in chunks for _ in range(reps)], key=lambda c: -c[0].size), reps
 
 

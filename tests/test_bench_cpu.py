@@ -24,8 +24,8 @@ def tiny_samples():
 def test_process_jobs_cover_the_sample():
     samples = tiny_samples()
     jobs, reps = bench.proc_jobs(samples, 8)
-    # clips of at most 8 frames: 5 | 8 + 3 frames -> 3 chunks, 3 copies to fill 8 workers
-    assert reps == 3 and len(jobs) == 9
+    # clips of at most 8 frames: 5 | 8 + 3 frames -> 3 chunks, 11 copies for 4 jobs per worker
+    assert bench.PROC_JOBS_PER == 4 and reps == 11 and len(jobs) == 33
     assert all(a.shape[0] <= bench.PROC_CHUNK_F for a, _ in jobs)
     frames = sum(a.shape[0] for a, _ in jobs)
     assert frames == reps * sum(a.shape[0] for a, _ in samples)
