@@ -148,6 +148,35 @@ def test_block_matching_wide_windows(dev, oracle, channels):
         assert_bm_equal(gpu_similar(vid, p, dev), oracle.similar(p, vid), p)
 
 
+def grid_points(end, step):
+    # ind_initialize (src/Utilities/Utilities.cpp:400-415): 0, step, ... <= end, then end
+    pts = list(range(0, end + 1, step))
+    return pts if pts[-1] == end else pts + [end]
+
+
+@pytest.mark.parametrize("channels,step", [(1, 1), (3, 2)])
+def test_distance_count(dev, channels, step):
+    # the patch distances the block matching evaluates (the roofline's
+    # work count).  One frame: only the reference frame's clamped Ns x Ns
+    # window is searched, so the count is its area summed over the grid.
+    # Five frames: at least that per frame, at most Ns^2 + 2 Nf Nb Npr^2
+    # per reference patch.
+    p = vb.default_params(step, 20.0)
+    w, h, half = 61, 43, (p.Ns - 1) // 2
+    rng = np.random.default_rng(5 + channels)
+    vid = rng.normal(100, 20, (5, channels, h, w)).astype(np.float32)
+
+    def span(v, end):
+        return min(end, v + half) - max(0, v - half) + 1
+
+    one = sum(span(x, w - p.k) * span(y, h - p.k)
+              for y in grid_points(h - p.k, p.p) for x in grid_points(w - p.k, p.p))
+    assert vb.bm_distance_count(gpu(vid[:1], dev), p) == one
+    n = vb.bm_distance_count(gpu(vid, dev), p)
+    refs = vb.ref_count(p, vb.dims_of(vid))
+    assert 5 * one < n <= refs * (p.Ns ** 2 + 2 * p.Nf * p.Nb * p.Npr ** 2)
+
+
 def ratio(num, den, fb):
     return np.where(den == 0, fb, num / np.where(den == 0, 1, den)).astype(np.float32)
 

@@ -94,6 +94,22 @@ cudaError_t pool_alloc(T** p, size_t count, cudaStream_t s)
     return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), count * sizeof(T) + 16, pool, s);
 }
 
+// A pool allocation freed (stream-ordered) when it goes out of scope, so
+// that an early error return (CK) releases it too.
+template <class T>
+struct PoolBuf {
+    T* p = nullptr;
+    cudaStream_t s;
+    explicit PoolBuf(cudaStream_t st) : s(st) {}
+    PoolBuf(const PoolBuf&) = delete;
+    PoolBuf& operator=(const PoolBuf&) = delete;
+    cudaError_t alloc(size_t count) { return pool_alloc(&p, count, s); }
+    ~PoolBuf()
+    {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 // ind_size (src/Utilities/Utilities.cpp:441-458) for beginning = 0.
 unsigned grid_size(unsigned end, unsigned step)
 {
@@ -309,14 +325,12 @@ int run_step_pair(int step, const StepParams& P, const float* noisy, const float
                   const float* bflow, float* pair, cudaStream_t s)
 {
     const size_t n = (size_t)P.whc * P.F;
-    unsigned *tab_idx = nullptr, *tab_nsx = nullptr;
-    CK(pool_alloc(&tab_idx, (size_t)P.nrefs * P.N, s));
-    CK(pool_alloc(&tab_nsx, (size_t)P.nrefs, s));
+    PoolBuf<unsigned> tab_idx(s), tab_nsx(s);
+    CK(tab_idx.alloc((size_t)P.nrefs * P.N));
+    CK(tab_nsx.alloc((size_t)P.nrefs));
     CK(cudaMemsetAsync(pair, 0, 2 * n * sizeof(float), s));
-    CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx, nullptr, nullptr, tab_nsx, P.nrefs, s));
-    CK(launch_filter(step, P, noisy, basic, fflow, tab_idx, tab_nsx, nullptr, nullptr, pair, P.nrefs, s));
-    CK(cudaFreeAsync(tab_idx, s));
-    CK(cudaFreeAsync(tab_nsx, s));
+    CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx.p, nullptr, nullptr, tab_nsx.p, P.nrefs, s));
+    CK(launch_filter(step, P, noisy, basic, fflow, tab_idx.p, tab_nsx.p, nullptr, nullptr, pair, P.nrefs, s));
     return VBM3D_OK;
 }
 
@@ -474,12 +488,17 @@ int vbm3d_gpu_similar_patches(const vbm3d_params* prms, const float* video, cons
     if (!indexes && !distances && !nsimp && !nsx) return VBM3D_OK;
     if (!video) return fail(VBM3D_ERR_INVALID_ARGUMENT, "NULL video pointer");
     cudaStream_t s = (cudaStream_t)stream;
+    PoolBuf<unsigned> own_idx(s), own_ns(s);  // the tables the caller does not take
     unsigned *idx = indexes, *ns = nsx;
-    if (!idx) CK(pool_alloc(&idx, (size_t)P.nrefs * P.N, s));
-    if (!ns) CK(pool_alloc(&ns, (size_t)P.nrefs, s));
+    if (!idx) {
+        CK(own_idx.alloc((size_t)P.nrefs * P.N));
+        idx = own_idx.p;
+    }
+    if (!ns) {
+        CK(own_ns.alloc((size_t)P.nrefs));
+        ns = own_ns.p;
+    }
     CK(launch_bm(P, video, fflow, bflow, idx, distances, nsimp, ns, P.nrefs, s));
-    if (!indexes) CK(cudaFreeAsync(idx, s));
-    if (!nsx) CK(cudaFreeAsync(ns, s));
     return VBM3D_OK;
 }
 
@@ -491,17 +510,14 @@ int vbm3d_gpu_bm_distance_count(const vbm3d_params* prms, const float* video, co
     int rc = build_params(prms, dims, 0.f, 0, P);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    unsigned *idx = nullptr, *ns = nullptr;
-    unsigned long long* d_count = nullptr;
-    CK(pool_alloc(&idx, (size_t)P.nrefs * P.N, s));
-    CK(pool_alloc(&ns, (size_t)P.nrefs, s));
-    CK(pool_alloc(&d_count, 1, s));
-    CK(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), s));
-    CK(launch_bm(P, video, fflow, bflow, idx, nullptr, nullptr, ns, P.nrefs, s, d_count));
-    CK(cudaMemcpyAsync(count, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaFreeAsync(idx, s));
-    CK(cudaFreeAsync(ns, s));
-    CK(cudaFreeAsync(d_count, s));
+    PoolBuf<unsigned> idx(s), ns(s);
+    PoolBuf<unsigned long long> d_count(s);
+    CK(idx.alloc((size_t)P.nrefs * P.N));
+    CK(ns.alloc((size_t)P.nrefs));
+    CK(d_count.alloc(1));
+    CK(cudaMemsetAsync(d_count.p, 0, sizeof(unsigned long long), s));
+    CK(launch_bm(P, video, fflow, bflow, idx.p, nullptr, nullptr, ns.p, P.nrefs, s, d_count.p));
+    CK(cudaMemcpyAsync(count, d_count.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return VBM3D_OK;
 }
