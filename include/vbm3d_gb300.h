@@ -120,12 +120,16 @@ int vbm3d_gpu_step2(const vbm3d_params *prms, const float *noisy, const float *b
  * that every GPU using this library holds until the process exits; a call
  * needs (reference patches) * (N + 1) 4-byte words of it and returns
  * VBM3D_ERR_UNSUPPORTED when that exceeds 8 Mi words (for 1080p RGB with
- * the default step-1 parameters: at most 16 frames per call).  The first
- * call on a device looks up the array's device address; make that first
- * call before any stream capture.  All calls share the one array, so calls
- * whose GPU work overlaps (different streams, or different host threads on
- * one device) race: serialise them.  Same arguments and results as
- * vbm3d_gpu_step1. */
+ * the default step-1 parameters: at most 16 frames per call).  The driver
+ * reserves the 32 MiB when it loads the library's module: at context
+ * creation under CUDA_MODULE_LOADING=EAGER, at the first call of this
+ * entry point under lazy loading (the default); a caller with a strict
+ * memory budget makes one call at start-up.  The first call in a device
+ * context looks up the array's device address (again after a device reset,
+ * which reloads the module); make that first call before any stream
+ * capture.  All calls share the one array, so calls whose GPU work
+ * overlaps (different streams, or different host threads on one device)
+ * race: serialise them.  Same arguments and results as vbm3d_gpu_step1. */
 int vbm3d_gpu_step1_noalloc(const vbm3d_params *prms, const float *noisy,
                             const float *fflow, const float *bflow, vbm3d_dims dims,
                             float sigma, int color_space,

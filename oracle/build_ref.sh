@@ -1,7 +1,11 @@
 #!/bin/sh
 # Builds the reference's own hot-path sources into oracle/_ref/ (test
 # infrastructure).  Reads the sources where they lie; copies none of them.
-#   $1 = reference project root (default /root/reference)
+#   $1 = reference project root (default: $VBM3D_REFERENCE, else
+#        /root/reference, where this container mounts it)
+#   --where       print the reference project root and exit
+#   --if-present  build only if the reference sources are there (exit 0
+#                 quietly otherwise, as on machines without them)
 # Outputs:
 #   oracle/_ref/libvbm3d_ref_exact.so  -O2, no fast-math, no FP contraction:
 #       the parity oracle (IEEE float arithmetic in source order)
@@ -16,7 +20,20 @@
 #       the pin of the multiscaler restatement
 # FFTW3f is not installed: oracle/fftw_shim supplies REDFT10/REDFT01.
 set -e
-REF=${1:-/root/reference}
+MODE=""
+case "$1" in
+    --where|--if-present) MODE=$1; shift ;;
+esac
+REF=${1:-${VBM3D_REFERENCE:-/root/reference}}
+if [ "$MODE" = "--where" ]; then
+    echo "$REF"
+    exit 0
+fi
+if [ ! -d "$REF/src" ]; then
+    [ "$MODE" = "--if-present" ] && exit 0
+    echo "reference sources not found under $REF" >&2
+    exit 1
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

@@ -101,7 +101,14 @@ def test_status_strings(lib):
         assert lib.vbm3d_status_string(code).startswith(b"VBM3D_")
 
 
-REFERENCE_SRC = "/root/reference/src"
+def reference_src():
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    where = subprocess.check_output(["sh", os.path.join(root, "oracle", "build_ref.sh"), "--where"], text=True)
+    return os.path.join(where.strip(), "src")
+
+
+REFERENCE_SRC = reference_src()
 
 
 @pytest.mark.skipif(not os.path.isdir(REFERENCE_SRC), reason="reference sources not present")

@@ -1,10 +1,14 @@
 """The allocation-free step-1 entry point (vbm3d_gpu_step1_noalloc), for
 callers that cannot let the library allocate device memory: it must give the
-results of vbm3d_gpu_step1, call after call, with its fixed table.
+results of vbm3d_gpu_step1, call after call, with its fixed table, and the
+device's free memory must not drop during a call.
 
 Collected last on purpose: a failure here comes after every other test ran.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -70,3 +74,47 @@ def test_noalloc_rejects_oversized_calls(lib):
     fake = C.c_void_p(256)  # never dereferenced: the size check comes first
     rc = lib.vbm3d_gpu_step1_noalloc(C.byref(p), fake, None, None, Dims(w, h, f, c), 30.0, 1, fake, fake, None)
     assert rc == 2 and b"exceed" in lib.vbm3d_last_error()
+
+
+# Run in a fresh process, so that no earlier test's allocations hide one.
+# The kernels are warmed up first (vbm3d_gpu_step1 on a small clip, then
+# vbm3d_gpu_step1_noalloc on it, which loads the module holding the fixed
+# table); then one call on three 1080p RGB frames, whose 6.2 MB table a
+# pool allocation would have to reserve anew.
+FREE_MEMORY_PROBE = r"""
+import ctypes as C, sys, torch
+sys.path.insert(0, sys.argv[1])
+import vbm3d_gb300 as vb
+from vbm3d_gb300._abi import Dims
+L = vb.load()
+vp = C.c_void_p
+for fn in (L.vbm3d_gpu_step1, L.vbm3d_gpu_step1_noalloc):
+    fn.argtypes = [C.POINTER(vb.Params), vp, vp, vp, Dims, C.c_float, C.c_int, vp, vp, vp]
+def call(fn, x, num, den):
+    f, c, h, w = x.shape
+    p = vb.default_params(1, 30.0)
+    rc = fn(C.byref(p), vp(x.data_ptr()), None, None, Dims(w, h, f, c), 30.0, 1, vp(num.data_ptr()),
+            vp(den.data_ptr()), None)
+    assert rc == 0, L.vbm3d_last_error()
+g = torch.Generator(device="cuda").manual_seed(5)
+small = torch.rand((3, 3, 64, 80), device="cuda", generator=g) * 255
+big = torch.rand((3, 3, 1080, 1920), device="cuda", generator=g) * 255
+sn, sd, bn, bd = (torch.empty_like(small), torch.empty_like(small), torch.empty_like(big), torch.empty_like(big))
+call(L.vbm3d_gpu_step1, small, sn, sd)
+call(L.vbm3d_gpu_step1_noalloc, small, sn, sd)
+call(L.vbm3d_gpu_step1_noalloc, small, sn, sd)
+torch.cuda.synchronize()
+free0 = torch.cuda.mem_get_info()[0]
+call(L.vbm3d_gpu_step1_noalloc, big, bn, bd)
+torch.cuda.synchronize()
+free1 = torch.cuda.mem_get_info()[0]
+print("free memory drop: %d bytes" % (free0 - free1))
+assert free0 - free1 < (2 << 20), free0 - free1
+"""
+
+
+def test_noalloc_does_not_allocate(lib):
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = subprocess.run([sys.executable, "-c", FREE_MEMORY_PROBE, root], capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stdout + res.stderr

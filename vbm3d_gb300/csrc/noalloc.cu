@@ -8,14 +8,22 @@
 // own allocator, real-time pipelines that forbid any allocation once they
 // are running, and processes under a strict per-tenant memory budget.  For
 // them vbm3d_gpu_step1_noalloc runs the same two kernels with the table in
-// the fixed device array below and calls no allocating routine at all.
+// the fixed device array below and calls no cudaMalloc, cudaFree or other
+// allocating routine.
 //
 // The array is a file-scope __device__ object: every GPU on which this
-// library's kernels are loaded holds it (32 MiB) until the
-// process exits.  Host code cannot use the array's name as a device
-// address (in host code it names a host-side shadow); its device address is
-// looked up with cudaGetSymbolAddress once per device, with that device
-// current, and passed to the kernels.
+// library's module is loaded holds it (32 MiB) until the process exits.
+// The driver reserves it when it loads the module: at context creation
+// when module loading is eager (CUDA_MODULE_LOADING=EAGER), at the first
+// use of the module (the first call of this entry point, whose address
+// lookup loads it) under lazy loading, the default.  A caller with a strict
+// memory budget makes one call at start-up.  Host code cannot use the
+// array's name as a device address (in host code it names a host-side
+// shadow); its device address is looked up with cudaGetSymbolAddress once
+// per device context, with that device current, and passed to the kernels.
+// The lookup is cached per context (the driver's unique context id), so a
+// device reset or a re-created primary context, which reloads the module
+// at a new address, triggers a new lookup.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -44,13 +52,51 @@ __device__ __align__(256) unsigned g_noalloc_table[kNoAllocTableWords];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned* g_table_ptr[kMaxDevices] = {};
+unsigned long long g_table_ctx[kMaxDevices] = {};  // context id of each cached address
 
-// Looks up the device address of g_noalloc_table on the current device
-// (once per device).  The first call on a device performs this lookup.
+// The driver's id of the calling thread's current context (cuCtxGetCurrent,
+// cuCtxGetId through the runtime's driver entry points, so that the
+// library needs no link against the driver library).
+cudaError_t current_context_id(unsigned long long* id)
+{
+    typedef int (*GetCurrentFn)(void**);
+    typedef int (*GetIdFn)(void*, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return e;
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return cudaErrorNotSupported;
+        get_current = reinterpret_cast<GetCurrentFn>(f1);
+        get_id = reinterpret_cast<GetIdFn>(f2);
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0) return cudaErrorDeviceUninitialized;
+    if (!ctx) {
+        // no context yet on this thread: the runtime's first call would make
+        // the device's primary context current; cudaSetDevice does that now
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaSetDevice(dev);
+        if (e != cudaSuccess) return e;
+        if (get_current(&ctx) != 0 || !ctx) return cudaErrorDeviceUninitialized;
+    }
+    return get_id(ctx, id) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// Looks up the device address of g_noalloc_table on the current device,
+// once per device context (the first call in a context performs it).
 int table_for_current_device(unsigned** out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
+    unsigned long long ctx = 0;
+    if (e == cudaSuccess) e = current_context_id(&ctx);
     if (e != cudaSuccess) {
         vbm3d::set_last_error(VBM3D_ERR_CUDA, cudaGetErrorString(e));
         return VBM3D_ERR_CUDA;
@@ -60,7 +106,7 @@ int table_for_current_device(unsigned** out)
         return VBM3D_ERR_UNSUPPORTED;
     }
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_table_ptr[dev]) {
+    if (!g_table_ptr[dev] || g_table_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_table);
         if (e != cudaSuccess || !p) {
@@ -69,6 +115,7 @@ int table_for_current_device(unsigned** out)
             return VBM3D_ERR_CUDA;
         }
         g_table_ptr[dev] = static_cast<unsigned*>(p);
+        g_table_ctx[dev] = ctx;
     }
     *out = g_table_ptr[dev];
     return VBM3D_OK;

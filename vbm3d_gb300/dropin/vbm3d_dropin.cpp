@@ -2,8 +2,8 @@
 // src/vbm3d.h:25-70) that forwards to the GB300 library's C ABI.
 //
 // Build it inside the reference tree instead of src/vbm3d.cpp:
-//     g++ -std=c++11 -O2 -I<vbm3d>/src -I<vbm3d>/src/Utilities -I<this repo>/include \
-//         -c vbm3d_dropin.cpp
+//     g++ -std=c++11 -O2 -I<vbm3d>/src -I<vbm3d>/src/Utilities
+//         -I<this repo>/include -c vbm3d_dropin.cpp
 // and link libvbm3d_gb300.so.  main.cpp, run_vbm3d's callers and the
 // Video<float> / Parameters types stay unchanged.  FFTW plans are accepted
 // and ignored (the GPU needs none).  Differences from the reference:
@@ -15,10 +15,21 @@
 //    (src/vbm3d.cpp:467-468);
 //  * run_vbm3d leaves vid_noisy in RGB without the YUV round trip the
 //    reference applies to it in place.
+// Flows: an empty Video means zero flow.  A flow of the video's width and
+// height holds either F frames (the zero flows main.cpp builds when no flow
+// file is given, src/main.cpp:353-369) or F - 1 frames (what main.cpp loads
+// from flow files: fflow of frames first..last-1, bflow of first+1..last,
+// src/main.cpp:360, :369).  The steps never read a flow's frame F - 1
+// (forward chains stop at the last frame, backward chains read bflow[t - 1]),
+// so an F - 1-frame flow is passed as an F-frame buffer whose last frame is
+// zero.  Any other size is the mismatch main.cpp rejects
+// (src/main.cpp:372-376): VBM3D_ERR_SIZE_MISMATCH.
+#include <algorithm>
 #include <cassert>
 #include <cstdio>
 #include <cstdlib>
 #include <ctime>  // the reference headers use time() and assert() without including them
+#include <vector>
 
 #include "vbm3d.h"
 #include "vbm3d_gb300.h"
@@ -43,11 +54,38 @@ vbm3d_dims dims_of(const Video<float>& v)
     return d;
 }
 
-const float* flow_ptr(const Video<float>& f, const Video<float>& vid)
+// The flow buffer the C ABI reads (W*H*F*2 floats, or NULL for zero flow)
+// for flow f of video vid; `pad` holds the zero-padded copy of an
+// F - 1-frame flow.  Returns VBM3D_OK or VBM3D_ERR_SIZE_MISMATCH.
+int flow_arg(const Video<float>& f, const Video<float>& vid, std::vector<float>& pad, const float** out)
 {
-    if (f.sz.whcf == 0) return NULL;
-    if (f.sz.width != vid.sz.width || f.sz.height != vid.sz.height || f.sz.frames < vid.sz.frames) return NULL;
-    return f.data.data();
+    *out = NULL;
+    if (f.sz.whcf == 0) return VBM3D_OK;
+    if (f.sz.width != vid.sz.width || f.sz.height != vid.sz.height || f.sz.channels != 2)
+        return VBM3D_ERR_SIZE_MISMATCH;
+    if (f.sz.frames == vid.sz.frames) {
+        *out = f.data.data();
+        return VBM3D_OK;
+    }
+    if (f.sz.frames + 1 != vid.sz.frames) return VBM3D_ERR_SIZE_MISMATCH;
+    pad.assign((size_t)vid.sz.wh * 2 * vid.sz.frames, 0.f);
+    std::copy(f.data.begin(), f.data.begin() + (size_t)f.sz.whcf, pad.begin());
+    *out = pad.data();
+    return VBM3D_OK;
+}
+
+// Both flows of a call; prints the reason and returns the status on a
+// mismatch.
+int flow_args(const Video<float>& ff, const Video<float>& bf, const Video<float>& vid, std::vector<float>& fpad,
+              std::vector<float>& bpad, const float** fp, const float** bp)
+{
+    int rc = flow_arg(ff, vid, fpad, fp);
+    if (rc == VBM3D_OK) rc = flow_arg(bf, vid, bpad, bp);
+    if (rc != VBM3D_OK)
+        std::fprintf(stderr, "vbm3d_gb300: %s: flows of %ux%ux%u(x%u) / %ux%ux%u(x%u) for a %ux%ux%u video\n",
+                     vbm3d_status_string(rc), ff.sz.width, ff.sz.height, ff.sz.frames, ff.sz.channels, bf.sz.width,
+                     bf.sz.height, bf.sz.frames, bf.sz.channels, vid.sz.width, vid.sz.height, vid.sz.frames);
+    return rc;
 }
 
 void step(int which, const float sigma, const Video<float>& noisy, const Video<float>* basic,
@@ -61,13 +99,16 @@ void step(int which, const float sigma, const Video<float>& noisy, const Video<f
         return;
     }
     vbm3d_params p = to_c(prms);
-    int rc = vbm3d_step_host(which, &p, noisy.data.data(), basic ? basic->data.data() : NULL,
-                             flow_ptr(fflow, noisy), flow_ptr(bflow, noisy), dims_of(noisy), sigma,
-                             color_space ? 1 : 0, num.data.data(), den.data.data());
-    if (rc != VBM3D_OK) {
-        std::fprintf(stderr, "vbm3d_gb300: %s: %s\n", vbm3d_status_string(rc), vbm3d_last_error());
-        for (unsigned k = 0; k < num.sz.whcf; k++) num(k) = den(k) = 0.f;
+    std::vector<float> fpad, bpad;
+    const float *fp = NULL, *bp = NULL;
+    int rc = flow_args(fflow, bflow, noisy, fpad, bpad, &fp, &bp);
+    if (rc == VBM3D_OK) {
+        rc = vbm3d_step_host(which, &p, noisy.data.data(), basic ? basic->data.data() : NULL, fp, bp,
+                             dims_of(noisy), sigma, color_space ? 1 : 0, num.data.data(), den.data.data());
+        if (rc != VBM3D_OK) std::fprintf(stderr, "vbm3d_gb300: %s: %s\n", vbm3d_status_string(rc), vbm3d_last_error());
     }
+    if (rc != VBM3D_OK)
+        for (unsigned k = 0; k < num.sz.whcf; k++) num(k) = den(k) = 0.f;
 }
 
 }  // namespace
@@ -95,9 +136,11 @@ int run_vbm3d(const float sigma, Video<float>& vid_noisy, Video<float>& fflow, V
     if (vid_basic.sz != vid_noisy.sz) vid_basic.resize(vid_noisy.sz);
     if (vid_denoised.sz != vid_noisy.sz) vid_denoised.resize(vid_noisy.sz);
     vbm3d_params p1 = to_c(prms_1), p2 = to_c(prms_2);
-    int rc = vbm3d_run_host(sigma, vid_noisy.data.data(), flow_ptr(fflow, vid_noisy), flow_ptr(bflow, vid_noisy),
-                            vid_basic.data.data(), vid_denoised.data.data(), &p1, &p2, color_space ? 1 : 0,
-                            dims_of(vid_noisy));
+    std::vector<float> fpad, bpad;
+    const float *fp = NULL, *bp = NULL;
+    if (flow_args(fflow, bflow, vid_noisy, fpad, bpad, &fp, &bp) != VBM3D_OK) return EXIT_FAILURE;
+    int rc = vbm3d_run_host(sigma, vid_noisy.data.data(), fp, bp, vid_basic.data.data(), vid_denoised.data.data(),
+                            &p1, &p2, color_space ? 1 : 0, dims_of(vid_noisy));
     if (rc != VBM3D_OK) {
         std::fprintf(stderr, "vbm3d_gb300: %s: %s\n", vbm3d_status_string(rc), vbm3d_last_error());
         return EXIT_FAILURE;
