@@ -1,0 +1,159 @@
+"""GPU parity at the full-size clips of the acceptance bar: the CUDA path
+(through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Workloads (colour transform on, as the reference CLI's default):
+  * RGB 960x540x50, sigma 20 and 40, once with the DCT as step 1's 2D
+    transform and once with bior1.5 in both steps (step 2 then at k = 8,
+    p = 4, which bior1.5 needs: src/main.cpp:193-201); the sigma-20 bior1.5
+    case also carries the exact flows of the generator's moving grating;
+  * RGB 1920x1080x30, sigma 30, motion up to 6 px/frame, default parameters.
+
+Checked per workload, with the bars written here:
+  * block matching bit-exact (indices, distances, group sizes) on every
+    reference patch of the first, middle and last frames: step 1 on the noisy
+    clip in YUV, step 2 on the oracle's basic estimate; the number of those
+    references whose sorted distances hold a tie is reported (ties resolve in
+    the reference's std::partial_sort order here, so they are compared too);
+  * step 1 alone: basic estimate within 1e-3 max-abs (0-255 scale);
+  * step 2 alone, given the oracle's basic estimate: final within 1e-3;
+  * end to end (step 2 matching on the GPU's own basic estimate): PSNR within
+    0.01 dB of the oracle's; the final's max-abs difference and the share of
+    values above 1e-3 are reported.
+The oracle runs the reference's single-thread semantics (untiled grid,
+aggregation in the reference's order) on all host cores.  Each workload
+prints one `PARITY {...}` line with its figures.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import vbm3d_gb300 as vb  # noqa: E402
+from oracle.pyoracle import Oracle  # noqa: E402
+from vbm3d_gb300._abi import dims_of  # noqa: E402
+from vbm3d_gb300.synth import make_clip, psnr  # noqa: E402
+
+TOL = 1e-3
+THREADS = os.cpu_count() or 1
+
+
+def kwien8_bior(p):
+    # step 2 at k = 8 (p = k / 2, d = 3^2 255 / k^2, src/main.cpp:172-181) with bior1.5
+    return p.replace(k=8, p=4, d=float(np.float32(3.0 * 3.0 * 255.0 / 64.0)), T_2D=vb.BIOR)
+
+
+WORKLOADS = {
+    "960x540x50_s20_dct": dict(shape=(960, 540, 50), sigma=20.0, seed=2001, t2d="dct"),
+    "960x540x50_s20_bior_flow": dict(shape=(960, 540, 50), sigma=20.0, seed=2002, t2d="bior", flow=True),
+    "960x540x50_s40_dct": dict(shape=(960, 540, 50), sigma=40.0, seed=2003, t2d="dct"),
+    "960x540x50_s40_bior": dict(shape=(960, 540, 50), sigma=40.0, seed=2004, t2d="bior"),
+    "1920x1080x30_s30": dict(shape=(1920, 1080, 30), sigma=30.0, seed=3000, t2d="default", vmax=6.0),
+}
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    vb.load()
+    return torch.device("cuda:0")
+
+
+def ratio(num, den, fb):
+    return np.where(den == 0, fb, num / np.where(den == 0, 1, den)).astype(np.float32)
+
+
+def gpu(a, dev):
+    return None if a is None else torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def ties(dist, nsimp):
+    """References whose sorted distance list holds two equal values."""
+    n = dist.shape[1]
+    valid = np.arange(n)[None, :] < nsimp[:, None]
+    eq = (dist[:, 1:] == dist[:, :-1]) & valid[:, 1:]
+    return int(eq.any(axis=1).sum())
+
+
+def bm_check(o, p, video, ff, bf, dev):
+    """Bit-exact block matching on every reference of the first, middle and
+    last frames; returns (references compared, references with ties)."""
+    d = dims_of(video)
+    res = vb.similar_patches(gpu(video, dev), p, gpu(ff, dev), gpu(bf, dev))
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in res.items()}
+    got["idx"] = got["idx"].view(np.uint32)
+    per_frame = vb.ref_count(p, d) // (d.frames - p.kt + 1)
+    frames = sorted({0, (d.frames - p.kt) // 2, d.frames - p.kt})
+    rows = np.concatenate([np.arange(t * per_frame, (t + 1) * per_frame) for t in frames])
+    pidx = o.ref_indices(p, d)[rows]
+    want = o.similar(p, video, ff, bf, pidx=pidx)
+    n = want["nsimp"]
+    np.testing.assert_array_equal(got["nsimp"][rows].astype(np.uint32), n)
+    np.testing.assert_array_equal(got["nsx"][rows].astype(np.uint32), want["nsx"])
+    mask = np.arange(p.N)[None, :] < n[:, None]
+    np.testing.assert_array_equal(got["idx"][rows][mask], want["idx"][mask])
+    np.testing.assert_array_equal(got["dist"][rows][mask], want["dist"][mask])
+    return len(rows), ties(want["dist"], n)
+
+
+@pytest.mark.parametrize("name", list(WORKLOADS))
+def test_full_size_parity(dev, name):
+    w = WORKLOADS[name]
+    W, H, F = w["shape"]
+    sigma = w["sigma"]
+    clean, noisy, ff, bf = make_clip(W, H, F, 3, sigma, w["seed"], vmax=w.get("vmax", 3.0),
+                                     with_flow=w.get("flow", False))
+    o = Oracle()
+    p1, p2 = o.default_params(1, sigma), o.default_params(2, sigma)
+    if w["t2d"] == "dct":
+        p1 = p1.replace(T_2D=vb.DCT)
+    elif w["t2d"] == "bior":
+        p2 = kwien8_bior(p2) if p2.k != 8 else p2.replace(T_2D=vb.BIOR)
+    yuv = o.color_transform(noisy, True)
+    # the oracle, step by step in the working colour space
+    onum, oden = o.step(1, p1, sigma, yuv, None, ff, bf, True, threads=THREADS)
+    obasic = ratio(onum, oden, yuv)
+    o2n, o2d = o.step(2, p2, sigma, yuv, obasic, ff, bf, True, threads=THREADS)
+    ofinal = ratio(o2n, o2d, obasic)
+    of_rgb = o.color_transform(ofinal, False)
+    del onum, oden, o2n, o2d
+    out = dict(workload=name, p1_T2D=int(p1.T_2D), p2_k=int(p2.k), p2_T2D=int(p2.T_2D), flow=ff is not None)
+    # block matching, bit for bit
+    out["bm1_refs"], out["bm1_refs_with_ties"] = bm_check(o, p1, yuv, ff, bf, dev)
+    out["bm2_refs"], out["bm2_refs_with_ties"] = bm_check(o, p2, obasic, ff, bf, dev)
+    out["bm_mismatches"] = 0
+    # step 1 alone
+    num, den = vb.step1(gpu(yuv, dev), p1, sigma, gpu(ff, dev), gpu(bf, dev), True)
+    torch.cuda.synchronize()
+    gbasic = ratio(num.cpu().numpy(), den.cpu().numpy(), yuv)
+    del num, den
+    out["step1_basic_maxabs"] = float(np.abs(gbasic - obasic).max())
+    # step 2 alone, given the oracle's basic estimate
+    num, den = vb.step2(gpu(yuv, dev), gpu(obasic, dev), p2, sigma, gpu(ff, dev), gpu(bf, dev), True)
+    torch.cuda.synchronize()
+    gfinal = ratio(num.cpu().numpy(), den.cpu().numpy(), obasic)
+    del num, den
+    out["step2_final_maxabs"] = float(np.abs(gfinal - ofinal).max())
+    # end to end on the GPU
+    x = gpu(noisy, dev)
+    gb, gf = vb.run(x, sigma, p1, p2, gpu(ff, dev), gpu(bf, dev), True)
+    torch.cuda.synchronize()
+    gb, gf = gb.cpu().numpy(), gf.cpu().numpy()
+    del x
+    d = np.abs(gf - of_rgb)
+    out["e2e_final_maxabs"] = float(d.max())
+    out["e2e_final_share_above_1e-3"] = float((d > TOL).mean())
+    out["psnr_noisy"] = psnr(clean, noisy)
+    out["psnr_basic_gpu"], out["psnr_basic_oracle"] = psnr(clean, gb), psnr(clean, o.color_transform(obasic, False))
+    out["psnr_final_gpu"], out["psnr_final_oracle"] = psnr(clean, gf), psnr(clean, of_rgb)
+    out["psnr_delta"] = abs(out["psnr_final_gpu"] - out["psnr_final_oracle"])
+    print("PARITY " + json.dumps(out))
+    assert out["step1_basic_maxabs"] <= TOL
+    assert out["step2_final_maxabs"] <= TOL
+    assert out["psnr_delta"] <= 0.01
+    assert abs(out["psnr_basic_gpu"] - out["psnr_basic_oracle"]) <= 0.01
