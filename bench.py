@@ -24,8 +24,13 @@ Multi-GPU: the path has no exchange step; --gpus N runs N independent
 replicas (one per rank) and value = total clip frames / max time.
 
 --impl reference times the reference's CPU implementation of the path on
-the host cores instead: the oracle port (oracle/vbm3d_oracle.c), each step a
-bounded sample of the same workload.  The CPU figure (that line's value and
+the host cores instead: the oracle port (oracle/vbm3d_oracle.c) built with
+the reference's own flags (-O3 -ffast-math -fomit-frame-pointer, OpenMP;
+oracle/_build/liboracle_fast.so), each step a bounded sample of the same
+workload.  The reference's sources are not on the GPU host; where they are,
+oracle/time_ref_vs_port.py times this build against the reference's own
+build on the same sample, and the line carries that measured ratio
+(profiles/cpu_reference_vs_port.json) as port_vs_reference.  The CPU figure (that line's value and
 the GPU line's cpu_baseline) is the higher of two modes: all host threads
 on one clip at a time (OpenMP), and independent clips of at most 8 frames
 as concurrent single-threaded processes, one per host thread, with at
@@ -107,10 +112,10 @@ def cpu_threads():
 
 
 def time_cpu(samples, steps=1):
-    """Oracle port over [(noisy, sigma)] with all host threads; returns
-    (Mpix-frames/s, threads)."""
-    from oracle.pyoracle import Oracle
-    o = Oracle()
+    """Oracle port (reference flags) over [(noisy, sigma)] with all host
+    threads; returns (Mpix-frames/s, threads)."""
+    from oracle.pyoracle import ORACLE_FAST_SO, Oracle
+    o = Oracle(ORACLE_FAST_SO)
     th = cpu_threads()
     mpf = 0.0
     t0 = time.perf_counter()
@@ -124,16 +129,16 @@ def time_cpu(samples, steps=1):
 
 
 def _port_warm(_):
-    from oracle.pyoracle import Oracle
-    Oracle()
+    from oracle.pyoracle import ORACLE_FAST_SO, Oracle
+    Oracle(ORACLE_FAST_SO)
     return 0
 
 
 def _port_job(job):
     """One clip through the oracle port on one thread (a worker process)."""
     noisy, sigma = job
-    from oracle.pyoracle import Oracle
-    o = Oracle()
+    from oracle.pyoracle import ORACLE_FAST_SO, Oracle
+    o = Oracle(ORACLE_FAST_SO)
     o.run(sigma, noisy, o.default_params(1, sigma), o.default_params(2, sigma), color_space=COLOR, threads=1)
     f, _, h, w = noisy.shape
     return w * h * f / 1e6
@@ -169,6 +174,19 @@ def time_cpu_procs(samples, steps=1):
     return mpf / dt, th, reps
 
 
+def port_vs_reference():
+    """The measured ratio of this port build to the reference's own build on
+    the same samples and threads (oracle/time_ref_vs_port.py, committed in
+    profiles/cpu_reference_vs_port.json), or None."""
+    path = os.path.join(ROOT, "profiles", "cpu_reference_vs_port.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = json.load(f)
+    return {"host": m["host"], "source": "profiles/cpu_reference_vs_port.json",
+            "port_fast_over_reference": {w: r["port_fast_over_reference"] for w, r in m["workloads"].items()}}
+
+
 def cpu_baseline(samples, desc, steps=1):
     """cpu_baseline of the JSON line: the oracle port on the host cores in
     two modes, all threads on one clip at a time (OpenMP) and independent
@@ -176,6 +194,9 @@ def cpu_baseline(samples, desc, steps=1):
     v_omp, th = time_cpu(samples, steps)
     v_proc, npr, reps = time_cpu_procs(samples, steps)
     return {"value": round(max(v_omp, v_proc), 4), "unit": UNIT, "cores": th, "kind": "port",
+            "build": "oracle/vbm3d_oracle.c with the reference's flags (-O3 -ffast-math -fomit-frame-pointer "
+                     "-fopenmp)",
+            "port_vs_reference": port_vs_reference(),
             "sample": desc + "; the higher of two modes",
             "modes": {"openmp": {"value": round(v_omp, 4), "threads": th},
                       "processes": {"value": round(v_proc, 4), "processes": npr,
@@ -596,6 +617,12 @@ def run_gpu(args):
         if rank == 0 and not args.no_cpu_baseline:
             samples, desc = cpu_sample("batch64", clips=clips)
             cpu = cpu_baseline(samples, desc)
+            if extra_1080 is not None:
+                # the 1080p30 clip's own CPU sample (a 480x270x30 centre crop)
+                samples, desc = cpu_sample("1080p30", noisy=noisy)
+                c1080 = cpu_baseline(samples, desc)
+                extra_1080["cpu_baseline"] = c1080
+                extra_1080["vs_cpu"] = round(extra_1080["value"] / c1080["value"], 1)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",

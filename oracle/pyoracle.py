@@ -3,7 +3,9 @@
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
 this module, as the checker; the product path never imports it.
 
-* `Oracle`   : the C restatement in oracle/vbm3d_oracle.c (oracle/_build).
+* `Oracle`   : the C restatement in oracle/vbm3d_oracle.c (oracle/_build);
+               Oracle(ORACLE_FAST_SO) is the same code built with the
+               reference's -O3 -ffast-math flags, for CPU timing only.
 * `RefLib`   : the reference's own sources compiled by oracle/build_ref.sh
                into oracle/_ref (present only where the reference sources
                were available at build time).
@@ -18,6 +20,7 @@ from vbm3d_gb300._abi import Dims, Params, dims_of
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+ORACLE_FAST_SO = os.path.join(HERE, "_build", "liboracle_fast.so")
 REF_EXACT_SO = os.path.join(HERE, "_ref", "libvbm3d_ref_exact.so")
 REF_FAST_SO = os.path.join(HERE, "_ref", "libvbm3d_ref_fast.so")
 
