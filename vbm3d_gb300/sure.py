@@ -66,3 +66,46 @@ def mc_sure(y, sigma_true, sigma_f, clean=None, stage="basic", probes=3, seed=0,
     if clean is not None:
         out["mse"] = float(((f.double() - clean.double()) ** 2).mean())
     return out
+
+
+def sure_step2_fixed_basic(y, sigma_true, sigma_f, basic, clean=None, probes=2, seed=0, p2=None):
+    """SURE of step 2 (Wiener) run at sigma_f with the basic estimate held
+    fixed: `basic` is given in the working colour space (YUV for RGB input)
+    and does not depend on y.  Then the estimate f(y) = T^-1 L T y is exactly
+    linear in y (groups and Wiener gains come from `basic`; aggregation is
+    linear), so b^T J b with J = T^-1 L T is an unbiased estimate of its
+    divergence and SURE is unbiased for its MSE.  Returns sure (linearised
+    divergence), sure_fd (finite-difference divergence, for comparison) and,
+    when `clean` is given, the true MSE."""
+    p2 = vb.default_params(2, sigma_f) if p2 is None else p2
+    rgb = y.shape[1] == 3
+
+    def estimate(v):
+        vv = vb.color_transform(v.clone(), True) if rgb else v.clone()
+        out = vb.normalize(*vb.step2(vv, basic, p2, sigma_f, color_space=True), basic)
+        return (vb.color_transform(out.clone(), False) if rgb else out), vv
+
+    f, yy = estimate(y)
+    L = vb.LinearStep(2, yy, sigma_f, p2, basic=basic, color_space=True)
+    gen = torch.Generator(device=y.device).manual_seed(seed)
+    eps = sigma_true / 20.0
+    div_lin = div_fd = 0.0
+    for _ in range(probes):
+        b = torch.randn(y.shape, generator=gen, device=y.device)
+        tb = vb.color_transform(b.clone(), True) if rgb else b
+        jb = L.apply(tb)
+        jb = vb.color_transform(jb, False) if rgb else jb
+        div_lin += float((b.double() * jb.double()).sum())
+        fe, _ = estimate(y + eps * b)
+        div_fd += float((b.double() * (fe.double() - f.double())).sum()) / eps
+    L.close()
+    div_lin /= probes
+    div_fd /= probes
+    n = y.numel()
+    res = float(((f.double() - y.double()) ** 2).sum()) / n
+    out = dict(sigma_f=sigma_f, div=div_lin, div_fd=div_fd,
+               sure=res - sigma_true ** 2 + 2 * sigma_true ** 2 * div_lin / n,
+               sure_fd=res - sigma_true ** 2 + 2 * sigma_true ** 2 * div_fd / n)
+    if clean is not None:
+        out["mse"] = float(((f.double() - clean.double()) ** 2).mean())
+    return out
