@@ -135,6 +135,26 @@ int vbm3d_gpu_step1_noalloc(const vbm3d_params *prms, const float *noisy,
                             float sigma, int color_space,
                             float *numerator, float *denominator, void *stream);
 
+/* Aggregation mode of the plain path, process-wide (no counterpart in the
+ * reference, whose single-thread run_vbm3d is deterministic by
+ * construction).  Off (0, the default): groups add into numerator /
+ * denominator with float atomics, so the order of the additions, and the
+ * last bits of the sums, vary from run to run.  On (1): the filter keeps
+ * every group's weighted estimates and one ordered pass sums them, at
+ * every pixel, in the reference's order (reference patches in grid order,
+ * then group members, src/vbm3d.cpp:612-650, :860-924): runs are
+ * bit-reproducible and, where the per-group estimates are the reference's
+ * own bits (the bior1.5 / Haar hard-threshold step), the step's numerator
+ * and denominator are the reference's to the bit.  Applies to
+ * vbm3d_gpu_step1 / _step2 / _run / _run_host / vbm3d_step_host (k in
+ * {7, 8}, kt == 1, N <= 8, else VBM3D_ERR_UNSUPPORTED while it is on);
+ * not to vbm3d_gpu_step1_noalloc, the batched form or the linearised form,
+ * which always add with atomics.  Costs device memory for the estimates:
+ * (reference patches) * C * N * k^2 floats per step (32 GB for step 2 of a
+ * 1920x1080x30 RGB clip). */
+int vbm3d_set_deterministic(int on);
+int vbm3d_get_deterministic(void);
+
 /* out[i] = denominator[i] == 0 ? fallback[i] : numerator[i] / denominator[i]
  * over `count` floats: the division in run_vbm3d (src/vbm3d.cpp:168-170,
  * :198-202).  `out` may alias `numerator`. */

@@ -14,11 +14,21 @@ Checked per workload, with the bars written here:
     clip in YUV, step 2 on the oracle's basic estimate; the number of those
     references whose sorted distances hold a tie is reported (ties resolve in
     the reference's std::partial_sort order here, so they are compared too);
-  * step 1 alone: basic estimate within 1e-3 max-abs (0-255 scale);
+  * step 1 alone: with bior1.5 (the default at k = 8), whose transform is
+    the reference's own float arithmetic, the basic estimate within 1e-3
+    max-abs (0-255 scale); with the DCT, whose float values differ from the
+    FFTW definition's by rounding, a coefficient within rounding of the hard
+    threshold can be kept on one side and zeroed on the other, which moves
+    that group's estimate by up to the threshold: the share of values off by
+    more than 1e-3 is reported and bounded (<= 1e-4), and PSNR holds;
   * step 2 alone, given the oracle's basic estimate: final within 1e-3;
   * end to end (step 2 matching on the GPU's own basic estimate): PSNR within
     0.01 dB of the oracle's; the final's max-abs difference and the share of
-    values above 1e-3 are reported.
+    values above 1e-3 are reported;
+  * end to end in the deterministic aggregation mode (vbm3d_set_deterministic)
+    with bior1.5 in step 1: the basic estimate is the oracle's to the bit, so
+    step 2 matches on the same basic estimate and the final estimate is
+    within 1e-3 at every value.
 The oracle runs the reference's single-thread semantics (untiled grid,
 aggregation in the reference's order) on all host cores.  Each workload
 prints one `PARITY {...}` line with its figures.
@@ -132,7 +142,10 @@ def test_full_size_parity(dev, name):
     torch.cuda.synchronize()
     gbasic = ratio(num.cpu().numpy(), den.cpu().numpy(), yuv)
     del num, den
-    out["step1_basic_maxabs"] = float(np.abs(gbasic - obasic).max())
+    d1 = np.abs(gbasic - obasic)
+    out["step1_basic_maxabs"] = float(d1.max())
+    out["step1_basic_share_above_1e-3"] = float((d1 > TOL).mean())
+    del d1
     # step 2 alone, given the oracle's basic estimate
     num, den = vb.step2(gpu(yuv, dev), gpu(obasic, dev), p2, sigma, gpu(ff, dev), gpu(bf, dev), True)
     torch.cuda.synchronize()
@@ -152,8 +165,24 @@ def test_full_size_parity(dev, name):
     out["psnr_basic_gpu"], out["psnr_basic_oracle"] = psnr(clean, gb), psnr(clean, o.color_transform(obasic, False))
     out["psnr_final_gpu"], out["psnr_final_oracle"] = psnr(clean, gf), psnr(clean, of_rgb)
     out["psnr_delta"] = abs(out["psnr_final_gpu"] - out["psnr_final_oracle"])
+    if p1.T_2D == vb.BIOR:
+        # the deterministic aggregation: the reference's order of additions
+        with vb.Deterministic(True):
+            x = gpu(noisy, dev)
+            db, df = vb.run(x, sigma, p1, p2, gpu(ff, dev), gpu(bf, dev), True)
+            torch.cuda.synchronize()
+            db, df = db.cpu().numpy(), df.cpu().numpy()
+            del x
+        out["det_basic_equal"] = bool(np.array_equal(db, o.color_transform(obasic, False)))
+        out["det_basic_maxabs"] = float(np.abs(db - o.color_transform(obasic, False)).max())
+        out["det_final_maxabs"] = float(np.abs(df - of_rgb).max())
     print("PARITY " + json.dumps(out))
-    assert out["step1_basic_maxabs"] <= TOL
+    if p1.T_2D == vb.BIOR:
+        assert out["step1_basic_maxabs"] <= TOL
+        assert out["det_basic_equal"]
+        assert out["det_final_maxabs"] <= TOL
+    else:
+        assert out["step1_basic_share_above_1e-3"] <= 1e-4
     assert out["step2_final_maxabs"] <= TOL
     assert out["psnr_delta"] <= 0.01
     assert abs(out["psnr_basic_gpu"] - out["psnr_basic_oracle"]) <= 0.01

@@ -15,6 +15,7 @@ Entry points mirror the reference's hot path (tehret/vbm3d):
   tvl1_flow(...), tvl1_video(...)    tvl1flow's TV-L1 (Dual_TVL1_optic_flow_multiscale), frame pairs / a clip
   run(...) / run_host(...)           run_vbm3d (src/vbm3d.cpp:87-376), device / host buffers
 Beside them, with no reference counterpart:
+  set_deterministic(on), Deterministic()  reference-order, bit-reproducible aggregation
   Batch(...)                         many uneven clips in one CUDA graph (vbm3d_batch_*)
   LinearStep(...)                    frozen linearisation and adjoint of a step (vbm3d_linear_*)
 """
@@ -80,6 +81,8 @@ def load(path=LIB_PATH):
     L.vbm3d_gpu_ms_recompose.argtypes = [C.POINTER(vp), C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_float, vp, vp]
     L.vbm3d_gpu_ms_merge_coarse.argtypes = [vp, vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_float,
                                             vp, vp]
+    L.vbm3d_set_deterministic.argtypes = [C.c_int]
+    L.vbm3d_get_deterministic.argtypes = []
     L.vbm3d_status_string.restype = C.c_char_p
     L.vbm3d_last_error.restype = C.c_char_p
     _lib = L
@@ -89,6 +92,33 @@ def load(path=LIB_PATH):
 def _check(rc):
     if rc != 0:
         raise VBM3DError(rc, load().vbm3d_last_error().decode())
+
+
+def set_deterministic(on):
+    """Aggregation mode of the plain path (vbm3d_set_deterministic): True
+    sums every pixel's terms in the reference's order (bit-reproducible
+    runs); False (the default) adds with float atomics."""
+    _check(load().vbm3d_set_deterministic(int(bool(on))))
+
+
+def deterministic():
+    return bool(load().vbm3d_get_deterministic())
+
+
+class Deterministic:
+    """Context manager: the plain path in the deterministic mode inside."""
+
+    def __init__(self, on=True):
+        self.on = on
+
+    def __enter__(self):
+        self.prev = deterministic()
+        set_deterministic(self.on)
+        return self
+
+    def __exit__(self, *exc):
+        set_deterministic(self.prev)
+        return False
 
 
 def default_params(step, sigma):

@@ -17,8 +17,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libvbm3d_gb300.so")
-SOURCES = ["api.cu", "batch.cu", "batch_step1.cu", "batch_step2.cu", "bm.cu", "bm2.cu", "filter.cu", "linear.cu",
-           "misc.cu", "multiscaler.cu", "noalloc.cu", "tvl1.cu"]
+SOURCES = ["api.cu", "batch.cu", "batch_step1.cu", "batch_step2.cu", "bm.cu", "bm2.cu", "det_agg.cu", "filter.cu",
+           "linear.cu", "misc.cu", "multiscaler.cu", "noalloc.cu", "tvl1.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-I" + os.path.join(ROOT, "include")]

@@ -5,9 +5,11 @@
 // bases, the DCT matrices, the noise table of estimate_sigma), owns the
 // scratch memory of a step (block-matching table) in a stream-ordered pool,
 // and launches the kernels on the caller's stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -29,6 +31,13 @@ cudaError_t launch_normalize_pair(const float* pair, const float* fb, float* out
 cudaError_t launch_normalize(const float* num, const float* den, const float* fb, float* out, size_t n,
                              cudaStream_t s);
 cudaError_t launch_color(float* v, unsigned wh, unsigned frames, int forward, cudaStream_t s);
+cudaError_t launch_filter_store(int step, const StepParams& P, const float* noisy, const float* basic,
+                                const unsigned* tab_idx, const unsigned* tab_nsx, float* est, float* wts,
+                                long long count, cudaStream_t stream);
+size_t det_scratch_words(const StepHead& P);
+cudaError_t launch_det_aggregate(const StepParams& P, const unsigned* tab_idx, const unsigned* tab_nsx,
+                                 const float* est, const float* wts, unsigned* scratch, float* pair,
+                                 cudaStream_t s);
 }  // namespace vbm3d
 
 using namespace vbm3d;
@@ -316,11 +325,47 @@ int build_params(const vbm3d_params* p, vbm3d_dims d, float sigma, int color_spa
         }
     P.bm_warp_bytes = bm_warp_bytes(P, P.bm_list_cap, P.bm_best_cap, P.bm_win_cap);
     P.neg_zero = -0.0f;
+    // Aggregation bands: a band's groups add into the 2 Nf + 1 frames around
+    // each frame of it, over its rows plus the search reach; size the band so
+    // that these (num, den) rows (8 bytes per value) take about 32 MB of L2.
+    {
+        const double frames = 2.0 * p->Nf + p->kt;
+        const double reach = (double)p->Ns / 2 + (double)p->Nf * p->Npr / 2 + p->k;
+        const double rows_px = 32e6 / (8.0 * d.width * d.channels * frames) - 2.0 * reach;
+        P.band_rows = std::max(4, (int)(rows_px / p->p));
+        if (P.band_rows >= P.nrows) P.band_rows = 0;
+    }
+    return VBM3D_OK;
+}
+
+// Aggregation mode of the plain path (vbm3d_set_deterministic).
+std::atomic<int> g_deterministic{0};
+
+// One step with the deterministic aggregation (det_agg.cu): the filter
+// keeps every group's weighted estimates, then one ordered pass sums them
+// into `pair`, in the reference's order.
+int run_step_pair_det(int step, const StepParams& P, const float* noisy, const float* basic, const float* fflow,
+                      const float* bflow, const unsigned* tab_idx, const unsigned* tab_nsx, float* pair,
+                      cudaStream_t s)
+{
+    (void)fflow;
+    (void)bflow;
+    if (!((P.k == 7 || P.k == 8) && P.kt == 1 && P.N <= 8))
+        return fail(VBM3D_ERR_UNSUPPORTED, "deterministic aggregation: k in {7, 8}, kt == 1 and N <= 8 only");
+    if (P.nrefs >= (1ll << 29) || P.W >= 65536 || P.H >= 65536)
+        return fail(VBM3D_ERR_UNSUPPORTED, "deterministic aggregation: video too large for its 32-bit keys");
+    PoolBuf<float> est(s), wts(s);
+    PoolBuf<unsigned> scr(s);
+    CK(est.alloc((size_t)P.nrefs * P.C * P.N * P.k * P.k));
+    CK(wts.alloc((size_t)P.nrefs * P.C));
+    CK(scr.alloc(det_scratch_words(P)));
+    CK(launch_filter_store(step, P, noisy, basic, tab_idx, tab_nsx, est.p, wts.p, P.nrefs, s));
+    CK(launch_det_aggregate(P, tab_idx, tab_nsx, est.p, wts.p, scr.p, pair, s));
     return VBM3D_OK;
 }
 
 // One step into the interleaved (numerator, denominator) accumulator
-// `pair` (2 floats per video value), which it zeroes first.  P is validated.
+// `pair` (2 floats per video value), which it overwrites.  P is validated.
 int run_step_pair(int step, const StepParams& P, const float* noisy, const float* basic, const float* fflow,
                   const float* bflow, float* pair, cudaStream_t s)
 {
@@ -328,8 +373,10 @@ int run_step_pair(int step, const StepParams& P, const float* noisy, const float
     PoolBuf<unsigned> tab_idx(s), tab_nsx(s);
     CK(tab_idx.alloc((size_t)P.nrefs * P.N));
     CK(tab_nsx.alloc((size_t)P.nrefs));
-    CK(cudaMemsetAsync(pair, 0, 2 * n * sizeof(float), s));
     CK(launch_bm(P, step == 1 ? noisy : basic, fflow, bflow, tab_idx.p, nullptr, nullptr, tab_nsx.p, P.nrefs, s));
+    if (g_deterministic.load())
+        return run_step_pair_det(step, P, noisy, basic, fflow, bflow, tab_idx.p, tab_nsx.p, pair, s);
+    CK(cudaMemsetAsync(pair, 0, 2 * n * sizeof(float), s));
     CK(launch_filter(step, P, noisy, basic, fflow, tab_idx.p, tab_nsx.p, nullptr, nullptr, pair, P.nrefs, s));
     return VBM3D_OK;
 }
@@ -423,6 +470,14 @@ int vbm3d_default_params(int step, float sigma, vbm3d_params* o)
     o->n = 16;
     return VBM3D_OK;
 }
+
+int vbm3d_set_deterministic(int on)
+{
+    g_deterministic.store(on ? 1 : 0);
+    return VBM3D_OK;
+}
+
+int vbm3d_get_deterministic(void) { return g_deterministic.load(); }
 
 int vbm3d_sigma_table(float sigma, unsigned channels, int color_space, float* t)
 {

@@ -261,11 +261,18 @@ std::vector<uint4> make_items(const vbm3d_batch& b, const WorkLaunch& w, int til
         const int c = w.clips[slot];
         const StepHead& P = b.ch[c].h[s];
         const long long per_frame = (long long)P.nrows * P.ncols;
-        for (int t = 0; t < P.nframes; t++)
-            for (long long r = 0; r < per_frame; r += tile, n++)
-                if (n % stride == 0)
-                    v.push_back(make_uint4((unsigned)c, (unsigned)(t * per_frame + r),
-                                           (unsigned)std::min<long long>(tile, per_frame - r), (unsigned)slot));
+        // filtering: rows in bands of band_rows, each band frame by frame
+        // (the aggregation order of band_order_ref); block matching: frames
+        const int band = (w.phase & 1) && P.band_rows > 0 ? P.band_rows : P.nrows;
+        for (int row0 = 0; row0 < P.nrows; row0 += band) {
+            const long long r0 = (long long)row0 * P.ncols;
+            const long long r1 = (long long)std::min(row0 + band, P.nrows) * P.ncols;
+            for (int t = 0; t < P.nframes; t++)
+                for (long long r = r0; r < r1; r += tile, n++)
+                    if (n % stride == 0)
+                        v.push_back(make_uint4((unsigned)c, (unsigned)(t * per_frame + r),
+                                               (unsigned)std::min<long long>(tile, r1 - r), (unsigned)slot));
+        }
     }
     return v;
 }

@@ -28,7 +28,7 @@ struct PWin {
     int tile;               // float offset of its staged tile
     int res;                // offset of its results in the phase result array
     int chain;              // 0: reference frame, 1: forward, 2: backward
-    int pad;
+    unsigned base;          // video offset of its top-left pixel in channel 0 (t*whc + y0*W + x0)
     unsigned long long seen;  // earlier windows on the same frame (bit i: scanned window i)
 };
 
@@ -455,6 +455,19 @@ __device__ __forceinline__ void store_entry(const StepHead& P, const Smem& S, co
     S.res[W.res + dy * W.ww + cx] = e;
 }
 
+// Waits for the staged channel c (its cp.async group: groups of channels
+// c + 1 .. C - 1 may still be in flight), then makes every lane's copies
+// of it visible to the group.
+template <int C, int G>
+__device__ __forceinline__ void wait_channel(int c, const Grp<G>& g)
+{
+    const int later = C - 1 - c;
+    if (later >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
+    else if (later == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 0;" ::: "memory");
+    g.sync();
+}
+
 // Distances of every position of the phase's nw windows.  Windows are
 // taken in pairs (0, 1), (2, 3), ...; a lane owns one slot (dy, 2cx) of a
 // pair and evaluates positions (dy, 2cx) and (dy, 2cx + 1) of both windows
@@ -525,6 +538,7 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
         if (pm) {
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
+                if (pass == 0) wait_channel<C>(c, g);
                 const float* pa = tA + c * plane;
                 const float* pb = tB + c * plane;
                 const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
@@ -552,6 +566,7 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
         } else {
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
+                if (pass == 0) wait_channel<C>(c, g);
                 const float* pa = tA + c * plane;
                 const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
 #pragma unroll 1
@@ -588,42 +603,42 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
 
 // Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
 // channels, at tile pitch `pitch`.  A warp copies two rows of a tile up to
-// 16 wide per step, a half warp one row (16 columns) per step.
+// 16 wide per step, a half warp one row (16 columns) per step.  The copies
+// go channel by channel, one cp.async group per channel, and are not
+// waited for here: phase_distances waits for channel c's group before it
+// reads channel c, so the later channels' copies are in flight while the
+// first channels' sums run.
 template <int K, int C, int G>
 __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, const Grp<G>& g,
                             int pitch, int plane)
 {
-    // every tile row of every window is copied asynchronously, then waited
-    // for once: the loads of the whole phase are in flight together.  The
-    // clip's geometry is read into registers before the first copy.
-    const long long W = P.W, wh = P.wh, whc = P.whc;
+    // the clip's geometry is read into registers before the first copy;
+    // video offsets fit 32 bits (W * H * F * C < 2^32)
+    const unsigned W = (unsigned)P.W, wh = P.wh;
     const unsigned tiles = smem_addr(S.tiles);
-    for (int w = 0; w < nw; w++) {
-        const PWin pwn = S.pw[w];
-        const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
-        int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
-        if (G == 32 && tw <= 16) {
-            x0 = g.gl & 15;
-            ystep = 2;
-            y0 = g.gl >> 4;
-        }
-        for (int x = x0; x < tw; x += xstep) {
-            const float* src = vid + pwn.t * whc + (pwn.y0 + y0) * W + pwn.x0 + x;
-            const unsigned dst = tiles + 4u * (unsigned)(pwn.tile + y0 * pitch + x);
-            const long long sstep = ystep * W;
-            const unsigned dstep = 4u * (unsigned)(ystep * pitch);
 #pragma unroll 1
-            for (int c = 0; c < C; c++) {
-                const float* s = src + c * wh;
-                unsigned d = dst + 4u * (unsigned)(c * plane);
+    for (int c = 0; c < C; c++) {
+        for (int w = 0; w < nw; w++) {
+            const PWin pwn = S.pw[w];
+            const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
+            int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
+            if (G == 32 && tw <= 16) {
+                x0 = g.gl & 15;
+                ystep = 2;
+                y0 = g.gl >> 4;
+            }
+            for (int x = x0; x < tw; x += xstep) {
+                const float* s = vid + (pwn.base + (unsigned)c * wh + (unsigned)y0 * W + (unsigned)x);
+                unsigned d = tiles + 4u * (unsigned)(pwn.tile + c * plane + y0 * pitch + x);
+                const unsigned sstep = (unsigned)ystep * W;
+                const unsigned dstep = 4u * (unsigned)(ystep * pitch);
 #pragma unroll 4
                 for (int y = y0; y < th; y += ystep, s += sstep, d += dstep) cp_async4s(d, s);
+                if (G == 32 && tw <= 16) break;  // the two half warps cover the 16 columns
             }
-            if (G == 32 && tw <= 16) break;  // the two half warps cover the 16 columns
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    g.sync();
 }
 
 // Registers the phase's windows in the list of scanned windows (after the
@@ -656,7 +671,7 @@ __device__ __forceinline__ PWin make_window(const StepHead& P, int t, int cx, in
     w.chain = chain;
     w.tile = 0;
     w.res = 0;
-    w.pad = 0;
+    w.base = (unsigned)t * P.whc + (unsigned)y0 * (unsigned)P.W + (unsigned)x0;
     w.seen = 0ull;
     return w;
 }

@@ -61,6 +61,9 @@ struct StepHead {
     // -0.0f, read by the kernels at run time (the addend of the exact
     // squaring FMA of block matching, which must not be a constant)
     float neg_zero;
+    // aggregation order: reference patches in bands of band_rows grid rows,
+    // each band through all frames (0: frames outer, the grid's order)
+    int band_rows;
 };
 
 // Transform tables of a step (k*k each, row-major, row stride k).
@@ -88,6 +91,26 @@ __device__ __forceinline__ void ref_coords(const StepHead& P, long long r, int& 
     const int ir = rem / P.ncols, jr = rem - ir * P.ncols;
     y = min(ir * P.p, P.H - P.k);
     x = min(jr * P.p, P.W - P.k);
+}
+
+// The i-th reference patch of the filtering order: bands of band_rows
+// grid rows, each band frame by frame, row by row.  A group adds into
+// frames t - Nf .. t + Nf near its reference patch, so the numerator /
+// denominator rows a band touches in all its frames stay in L2 while the
+// band is filtered, instead of being read back from DRAM once per frame
+// that reaches them.  A bijection of [0, nrefs).
+__device__ __forceinline__ long long band_order_ref(const StepHead& P, long long i)
+{
+    if (P.band_rows <= 0 || P.band_rows >= P.nrows) return i;
+    const long long per_band = (long long)P.band_rows * P.ncols * P.nframes;
+    const int band = (int)(i / per_band);
+    const long long rem = i - band * per_band;
+    const int row0 = band * P.band_rows;
+    const int rows = min(P.band_rows, P.nrows - row0);
+    const long long per_frame = (long long)rows * P.ncols;
+    const int t = (int)(rem / per_frame);
+    const long long in_frame = rem - t * per_frame;
+    return (long long)t * P.nrows * P.ncols + (long long)row0 * P.ncols + in_frame;
 }
 
 __device__ __forceinline__ unsigned patch_index(const StepHead& P, int x, int y, int t)

@@ -178,7 +178,7 @@ filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const
 {
     extern __shared__ __align__(16) float fsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    const long long r = band_order_ref(P, P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid);
     if (r >= P.nrefs) return;
 
     const int k = P.k, k2 = k * k, C = P.C, kt = P.kt;
@@ -242,7 +242,7 @@ filter_kernel_generic(const StepParams P, const float* __restrict__ noisy, const
     }
 }
 
-template <int STEP, int K, bool PAIR, int LPS>
+template <int STEP, int K, bool PAIR, int LPS, bool STORE = false>
 __global__ void __launch_bounds__(128, 4)
 filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float* __restrict__ basic,
                 const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx, const AggTarget A,
@@ -250,27 +250,27 @@ filter_kernel_k(const StepParams P, const float* __restrict__ noisy, const float
 {
     extern __shared__ __align__(16) float fsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long r = P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    const long long r = band_order_ref(P, P.ref_base + (long long)blockIdx.x * (blockDim.x >> 5) + wid);
     if (r >= P.nrefs) return;
-    filter_ref<STEP, K, PAIR, LPS>(P, P, r, fsm + (size_t)wid * warp_floats, lane, noisy, basic, tab_idx, tab_nsx,
-                                   A);
+    filter_ref<STEP, K, PAIR, LPS, STORE>(P, P, r, fsm + (size_t)wid * warp_floats, lane, noisy, basic, tab_idx,
+                                          tab_nsx, A);
 }
 
 namespace {
 
-template <int STEP, int K, bool PAIR, int LPS>
+template <int STEP, int K, bool PAIR, int LPS, bool STORE = false>
 cudaError_t launch_k_mode(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
                           const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
 {
     const int warps = 4;
     const int wf = kMaxN + (STEP == 1 ? 1 : 2) * P.C * P.N * (K * K + 1);
     const size_t smem = (size_t)warps * wf * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR, LPS>,
+    cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR, LPS, STORE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (count + warps - 1) / warps;
-    filter_kernel_k<STEP, K, PAIR, LPS><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic, tab_idx,
-                                                                                       tab_nsx, A, wf);
+    filter_kernel_k<STEP, K, PAIR, LPS, STORE><<<(unsigned)blocks, warps * 32, smem, stream>>>(P, noisy, basic,
+                                                                                              tab_idx, tab_nsx, A, wf);
     return cudaGetLastError();
 }
 
@@ -318,7 +318,34 @@ cudaError_t dispatch(const StepParams& P, const float* noisy, const float* basic
     return launch_generic<STEP, PAIR>(P, noisy, basic, fflow, tab_idx, tab_nsx, A, count, stream);
 }
 
+template <int STEP, int K>
+cudaError_t launch_k_store(const StepParams& P, const float* noisy, const float* basic, const unsigned* tab_idx,
+                           const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
+{
+    if (P.C == 1) return launch_k_mode<STEP, K, true, 4, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    return launch_k_mode<STEP, K, true, 1, true>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+}
+
 }  // namespace
+
+// The filter of the deterministic two-pass aggregation: instead of adding
+// into num / den, every group keeps its weighted estimates in est
+// ([nrefs][C][N][k*k]) and its weights in wts ([nrefs][C]); det_agg.cu sums
+// them in the reference's order.  k in {7, 8}, kt == 1, N <= 8.
+cudaError_t launch_filter_store(int step, const StepParams& P, const float* noisy, const float* basic,
+                                const unsigned* tab_idx, const unsigned* tab_nsx, float* est, float* wts,
+                                long long count, cudaStream_t stream)
+{
+    AggTarget A{nullptr, nullptr, nullptr};
+    A.est = est;
+    A.wts = wts;
+    if (P.N > 8 || P.kt != 1 || (P.k != 7 && P.k != 8)) return cudaErrorInvalidValue;
+    if (step == 1)
+        return P.k == 7 ? launch_k_store<1, 7>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
+                        : launch_k_store<1, 8>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+    return P.k == 7 ? launch_k_store<2, 7>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream)
+                    : launch_k_store<2, 8>(P, noisy, basic, tab_idx, tab_nsx, A, count, stream);
+}
 
 // Aggregates into num / den when `pair` is NULL, else into the interleaved
 // (num, den) array `pair` (2 floats per video value).

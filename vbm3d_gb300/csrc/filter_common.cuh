@@ -76,6 +76,11 @@ struct AggTarget {
     float* num;
     float* den;
     float* pair;
+    // deterministic two-pass aggregation (det_agg.cu): the weighted
+    // estimates kaiser * w * est of reference r in est[r][c][n][k*k] and its
+    // weights in wts[r][c], summed afterwards in the reference's order
+    float* est = nullptr;
+    float* wts = nullptr;
 };
 
 template <bool PAIR>
@@ -519,7 +524,7 @@ __device__ __forceinline__ void slice_fwd(const StepHead& P, const TT& T, float*
 // register-resident transforms for compile-time K (kt == 1, N <= 8), with
 // the warp's shared-memory region `base`.  T holds the kaiser / fwd / inv /
 // cn / cni tables (StepParams, or the batched form's compact copy).
-template <int STEP, int K, bool PAIR, int LPS, class TT>
+template <int STEP, int K, bool PAIR, int LPS, bool STORE = false, class TT>
 __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long long r, float* base, int lane,
                                            const float* __restrict__ noisy, const float* __restrict__ basic,
                                            const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
@@ -575,6 +580,23 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
 
     // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
     const int total = nsl * K2;
+    if (STORE) {
+        // the products the reference adds, kept for the ordered second pass:
+        // est[r][c][n][pq] = (kaiser[pq] * w_c) * est, the reference's
+        // evaluation order of kai * w * e (src/vbm3d.cpp:641-643)
+        float* er = A.est + (size_t)r * (size_t)(C * P.N * K2);
+        for (int e = lane; e < total; e += 32) {
+            const int sl = e / K2, pq = e - sl * K2;
+            const int c = sl >> log2n, n = sl & (nsx - 1);
+            er[((size_t)c * P.N + n) * K2 + pq] = (T.kaiser[pq] * wgt[c]) * ge[sl * SS + pq];
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < kMaxC; c++)
+                if (c < C) A.wts[(size_t)r * C + c] = wgt[c];
+        }
+        return;
+    }
     const size_t W = (size_t)P.W, wh = (size_t)P.wh;
     for (int e = lane; e < total; e += 32) {
         const int sl = e / K2, pq = e - sl * K2;
