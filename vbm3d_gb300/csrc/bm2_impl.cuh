@@ -430,11 +430,26 @@ __host__ __device__ __forceinline__ int bm2_tile_offset(int w, int tile_sz)
     return (w >> 1) * bm2_pair_stride(tile_sz) + (w & 1) * tile_sz;
 }
 
+// acc / norm rounded once, for this kernel's distance normalisations
+// (norm = k^2 C, one of 49, 64, 147, 192): q = acc * rcp with rcp the
+// rounded reciprocal, then Markstein's correction step with the exact
+// remainder acc - q norm (one FMA), q + (acc - q norm) rcp.  For these four
+// divisors the result equals the IEEE quotient acc / norm for every float
+// acc >= 2^-100 (tests/test_div_norm.py checks all of them); smaller,
+// infinite and NaN sums take the division itself.
+__device__ __forceinline__ float div_norm(float acc, float norm, float rcp)
+{
+    if (!(acc >= 0x1p-100f && acc <= 3.40282347e38f)) return __fdiv_rn(acc, norm);
+    const float q = __fmul_rn(acc, rcp);
+    const float r = __fmaf_rn(-q, norm, acc);
+    return __fmaf_rn(r, rcp, q);
+}
+
 // One phase entry: position (dy, cx) of window W with squared-difference
 // sum acc, unless it lies outside the window; an entry seen in an earlier
 // window of the same frame is stored as not a candidate (i == kNone).
 __device__ __forceinline__ void store_entry(const StepHead& P, const Smem& S, const PWin& W, int dy, int cx,
-                                            float acc, float norm, int rx, int ry, int rt)
+                                            float acc, float norm, float rcp, int rx, int ry, int rt)
 {
     if (dy >= W.wh || cx >= W.ww) return;
     const int qx = W.x0 + cx, qy = W.y0 + dy;
@@ -448,24 +463,11 @@ __device__ __forceinline__ void store_entry(const StepHead& P, const Smem& S, co
     }
     Pair e{0.f, kNone};
     if (!seen) {
-        float d = acc / norm;
+        float d = div_norm(acc, norm, rcp);
         if (qx == rx && qy == ry) d = d - P.dbias;
         e = Pair{d, pack_xyt(qx, qy, W.t, rt)};
     }
     S.res[W.res + dy * W.ww + cx] = e;
-}
-
-// Waits for the staged channel c (its cp.async group: groups of channels
-// c + 1 .. C - 1 may still be in flight), then makes every lane's copies
-// of it visible to the group.
-template <int C, int G>
-__device__ __forceinline__ void wait_channel(int c, const Grp<G>& g)
-{
-    const int later = C - 1 - c;
-    if (later >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
-    else if (later == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
-    else asm volatile("cp.async.wait_group 0;" ::: "memory");
-    g.sync();
 }
 
 // Distances of every position of the phase's nw windows.  Windows are
@@ -510,6 +512,7 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
     const int passes = pair_passes + (lone_slots + G - 1) / G;
     const float nz = P.neg_zero;
     const float norm = (float)(KK * C);
+    const float rcp = __frcp_rn(norm);
 
     for (int pass = 0; pass < passes; pass++) {
         const bool pm = pass < pair_passes;  // uniform over the group
@@ -538,7 +541,6 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
         if (pm) {
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
-                if (pass == 0) wait_channel<C>(c, g);
                 const float* pa = tA + c * plane;
                 const float* pb = tB + c * plane;
                 const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
@@ -566,7 +568,6 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
         } else {
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
-                if (pass == 0) wait_channel<C>(c, g);
                 const float* pa = tA + c * plane;
                 const float4* rr = reinterpret_cast<const float4*>(S.refp + c * K * KR);
 #pragma unroll 1
@@ -587,14 +588,14 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
             // pairs: (A dx, B dx, A dx+1, B dx+1) -> (a0x, a0y, a1x, a1y);
             // lone: (A dx, A dx+1) -> (a0x, a0y)
             const PWin A = S.pw[wa];
-            store_entry(P, S, A, dy, dx, a0x, norm, rx, ry, rt);
+            store_entry(P, S, A, dy, dx, a0x, norm, rcp, rx, ry, rt);
             if (pm) {
                 const PWin B = S.pw[wa + 1];
-                store_entry(P, S, B, dy, dx, a0y, norm, rx, ry, rt);
-                store_entry(P, S, A, dy, dx + 1, a1x, norm, rx, ry, rt);
-                store_entry(P, S, B, dy, dx + 1, a1y, norm, rx, ry, rt);
+                store_entry(P, S, B, dy, dx, a0y, norm, rcp, rx, ry, rt);
+                store_entry(P, S, A, dy, dx + 1, a1x, norm, rcp, rx, ry, rt);
+                store_entry(P, S, B, dy, dx + 1, a1y, norm, rcp, rx, ry, rt);
             } else {
-                store_entry(P, S, A, dy, dx + 1, a0y, norm, rx, ry, rt);
+                store_entry(P, S, A, dy, dx + 1, a0y, norm, rcp, rx, ry, rt);
             }
         }
     }
@@ -603,42 +604,46 @@ __device__ void phase_distances(const StepHead& P, const Smem& S, int nw, const 
 
 // Stages window tiles: rows y0 .. y0+wh+K-2, columns x0 .. x0+ww+K-2, all
 // channels, at tile pitch `pitch`.  A warp copies two rows of a tile up to
-// 16 wide per step, a half warp one row (16 columns) per step.  The copies
-// go channel by channel, one cp.async group per channel, and are not
-// waited for here: phase_distances waits for channel c's group before it
-// reads channel c, so the later channels' copies are in flight while the
-// first channels' sums run.
+// 16 wide per step, a half warp one row (16 columns) per step.  (Staging
+// channel by channel, one cp.async group each, with every channel's sums
+// starting when its copies land, measured 4-5 % slower on the RGB batch
+// launches: the per-window set-up then runs once per channel.)
 template <int K, int C, int G>
 __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __restrict__ vid, int nw, const Grp<G>& g,
                             int pitch, int plane)
 {
-    // the clip's geometry is read into registers before the first copy;
-    // video offsets fit 32 bits (W * H * F * C < 2^32)
+    // every tile row of every window is copied asynchronously, then waited
+    // for once: the loads of the whole phase are in flight together.  The
+    // clip's geometry is read into registers before the first copy; video
+    // offsets fit 32 bits (W * H * F * C < 2^32).
     const unsigned W = (unsigned)P.W, wh = P.wh;
     const unsigned tiles = smem_addr(S.tiles);
+    for (int w = 0; w < nw; w++) {
+        const PWin pwn = S.pw[w];
+        const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
+        int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
+        if (G == 32 && tw <= 16) {
+            x0 = g.gl & 15;
+            ystep = 2;
+            y0 = g.gl >> 4;
+        }
+        for (int x = x0; x < tw; x += xstep) {
+            const unsigned src = pwn.base + (unsigned)y0 * W + (unsigned)x;
+            const unsigned dst = tiles + 4u * (unsigned)(pwn.tile + y0 * pitch + x);
+            const unsigned sstep = (unsigned)ystep * W;
+            const unsigned dstep = 4u * (unsigned)(ystep * pitch);
 #pragma unroll 1
-    for (int c = 0; c < C; c++) {
-        for (int w = 0; w < nw; w++) {
-            const PWin pwn = S.pw[w];
-            const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
-            int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
-            if (G == 32 && tw <= 16) {
-                x0 = g.gl & 15;
-                ystep = 2;
-                y0 = g.gl >> 4;
-            }
-            for (int x = x0; x < tw; x += xstep) {
-                const float* s = vid + (pwn.base + (unsigned)c * wh + (unsigned)y0 * W + (unsigned)x);
-                unsigned d = tiles + 4u * (unsigned)(pwn.tile + c * plane + y0 * pitch + x);
-                const unsigned sstep = (unsigned)ystep * W;
-                const unsigned dstep = 4u * (unsigned)(ystep * pitch);
+            for (int c = 0; c < C; c++) {
+                const float* s = vid + (src + (unsigned)c * wh);
+                unsigned d = dst + 4u * (unsigned)(c * plane);
 #pragma unroll 4
                 for (int y = y0; y < th; y += ystep, s += sstep, d += dstep) cp_async4s(d, s);
-                if (G == 32 && tw <= 16) break;  // the two half warps cover the 16 columns
             }
+            if (G == 32 && tw <= 16) break;  // the two half warps cover the 16 columns
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    g.sync();
 }
 
 // Registers the phase's windows in the list of scanned windows (after the
