@@ -44,6 +44,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--tvl1", action="store_true", help="TV-L1 flows of a one-channel clip")
     ap.add_argument("--ms", type=int, default=0, help="multiscaler DCT pyramid with this many levels")
+    ap.add_argument("--bm-tile", type=int, default=FIXED["bm1_tile"], help="batched block matching: refs per item")
+    ap.add_argument("--bm-warps", type=int, default=FIXED["bm1_warps"], help="batched block matching: warps per block")
     a = ap.parse_args()
     if a.ms:
         _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
@@ -66,7 +68,8 @@ def main():
         for i, (w, h, f, c, s) in enumerate(batch_specs(scale=a.scale)[:a.batch]):
             _, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)
             clips.append(dict(noisy=torch.from_numpy(noisy).cuda(), sigma=s))
-        b = vb.Batch(clips, color_space=True, config=FIXED)
+        cfg = dict(FIXED, bm1_tile=a.bm_tile, bm2_tile=a.bm_tile, bm1_warps=a.bm_warps, bm2_warps=a.bm_warps)
+        b = vb.Batch(clips, color_space=True, config=cfg)
         for _ in range(a.runs):
             b.run()
         torch.cuda.synchronize()
