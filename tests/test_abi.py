@@ -141,7 +141,7 @@ def test_batch_rejects_bad_clips_before_any_cuda_call(lib):
     clips[1] = Clip(Dims(64, 48, 4, 2), 20.0, None, None, fake, None, None, None, fake)
     assert lib.vbm3d_batch_create(clips, 2, 1, None, C.byref(h), None) == 2
     clips[1] = Clip(Dims(64, 48, 4, 1), 20.0, None, None, fake, None, None, None, fake)
-    bad = BatchConfig(bm1_tile=4, bm1_warps=9)
+    bad = BatchConfig(bm1_tile=4, bm1_warps=3)
     assert lib.vbm3d_batch_create(clips, 2, 1, C.byref(bad), C.byref(h), None) == 1
     bad = BatchConfig(bm1_tile=4)
     assert lib.vbm3d_batch_create(clips, 2, 1, C.byref(bad), C.byref(h), None) == 1

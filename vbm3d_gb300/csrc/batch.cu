@@ -430,9 +430,9 @@ int tune_and_prepare(vbm3d_batch& b, const bool fixed[kPhases])
 {
     // candidates (refs per item, warps per block): one or two references
     // per warp and item for block matching, two to eight for filtering
-    static const PhaseCfg cand_bm[] = {{4, 4}, {8, 4}, {8, 8}, {16, 8}, {6, 3}};
+    static const PhaseCfg cand_bm[] = {{4, 4}, {8, 4}, {8, 8}, {16, 8}};
     static const PhaseCfg cand_f[] = {{16, 8}, {32, 8}, {16, 4}, {8, 4}};
-    constexpr int kCandBm = 5, kCandF = 4;
+    constexpr int kCandBm = 4, kCandF = 4;
     bool any = false;
     for (int ph = 0; ph < kPhases; ph++) any = any || !fixed[ph];
     cudaStream_t s = b.cs;
@@ -712,11 +712,11 @@ int vbm3d_batch_create(const vbm3d_clip* clips, int nclips, int color_space, con
                                    {config->filter2_tile, config->filter2_warps}};
         for (int ph = 0; ph < kPhases; ph++) {
             const int t = v[ph][0], w = v[ph][1];
-            if ((t != 0) != (w != 0) || t < 0 || t > 4096 || w < 0 || w > 8) {
+            if ((t != 0) != (w != 0) || t < 0 || t > 4096 || !(w == 0 || w == 1 || w == 2 || w == 4 || w == 8)) {
                 delete b;
                 return fail(VBM3D_ERR_INVALID_ARGUMENT,
-                            "phase %d: tile and warps must both be 0 (autotune) or both set, tile <= 4096, warps "
-                            "in 1 .. 8",
+                            "phase %d: tile and warps must both be 0 (autotune) or both set, tile <= 4096, warps in "
+                            "{1, 2, 4, 8}",
                             ph);
             }
             b->cfg[ph] = PhaseCfg{t, w};

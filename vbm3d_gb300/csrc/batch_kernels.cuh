@@ -51,7 +51,7 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // A reference patch takes a group of G lanes, as in bm2_kernel: a warp for
 // three channels, a half warp for one.
 template <int STEP, int K, int C, int G>
-__global__ void __maxnreg__(C == 3 ? 88 : 80)  // as bm2_kernel
+__global__ void __maxnreg__(C == 3 ? 96 : 80)  // as bm2_kernel
 batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
                 unsigned* __restrict__ head, int warp_bytes, const __grid_constant__ BmTable T)
 {

@@ -23,18 +23,19 @@ namespace vbm3d {
 
 namespace {
 
-// Register budget: 88 for three channels (no spills; shared memory limits
-// residency to 5 blocks of 4 warps, and 88 registers still allow 5, or 7
-// blocks of 3 warps, which the batched form's tuner may pick), 80 for one
-// channel (more resident blocks pay more).  A reference patch takes a
-// group of G lanes: a warp for three channels, a
-// half warp for one (whose distance sums are short, so the per-reference
-// bookkeeping a group runs once is shared by two references per warp).
+// Register budget: 96 for three channels (shared memory limits residency
+// to 5 blocks of 4 warps, so 96 registers cost no occupancy and remove
+// spills; 88, also spill-free, measured 2 % slower on the RGB batch
+// launches, and 7 blocks of 3 warps at 88 registers 17 % slower), 80 for
+// one channel (more resident blocks pay more).  A reference patch takes a
+// group of G lanes: a warp for three channels, a half warp for one (whose
+// distance sums are short, so the per-reference bookkeeping a group runs
+// once is shared by two references per warp).
 template <int K, int C>
 __host__ __device__ constexpr int bm2_group() { return C == 1 ? 16 : 32; }
 
 template <int K, int C>
-__global__ void __maxnreg__(C == 3 ? 88 : 80)
+__global__ void __maxnreg__(C == 3 ? 96 : 80)
 bm2_kernel(const StepParams P, const float* __restrict__ vid, const float* __restrict__ fflow,
            const float* __restrict__ bflow, unsigned* __restrict__ out_idx, float* __restrict__ out_dist,
            unsigned* __restrict__ out_nsimp, unsigned* __restrict__ out_nsx, const Layout L)
