@@ -344,10 +344,11 @@ def fp32_peak(dev, clocks):
 
 # DRAM bytes (read + write) per reference patch of the batched step-2 block
 # matching of the RGB k = 7 clips: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3, 32> on the full batch
-# (python -m vbm3d_gb300.profile_case --batch 64): 1.449 GB + 0.437 GB for
-# 12 308 991 reference patches.
-BM2_DRAM_BYTES_PER_REF = 153.0
+# dram__bytes_write.sum of batch_bm_kernel<2, 7, 3, 32> on the small case
+# (python -m vbm3d_gb300.profile_case --batch 16 --scale 0.5: 112.2 MB +
+# 24.5 MB for 973 383 reference patches), scaled by the launch's reference
+# patches.
+BM2_DRAM_BYTES_PER_REF = 137.0
 
 
 def timed(stream, fn, steps):
@@ -514,8 +515,9 @@ def run_gpu(args):
                                  bm["clips"]),
                     "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                    "traffic_source": "ncu DRAM bytes (read + write) of this kernel on the full batch, per "
-                                      "reference patch, x the launch's reference patches",
+                    "traffic_source": "ncu DRAM bytes (read + write) of this kernel per reference patch on "
+                                      "the small case (profile_case --batch 16 --scale 0.5), x the launch's "
+                                      "reference patches",
                     "peak_source": peak_src,
                     "algorithmic_flops": flops, "distances": n_dist, "refs": bm["refs"], "ms": round(bm["ms"], 2),
                     "share_of_run": round(bm["ms"] / sum(l["ms"] for l in launches), 3),
