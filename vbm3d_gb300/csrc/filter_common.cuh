@@ -142,6 +142,89 @@ __device__ __forceinline__ void col_pass(float* x, const float* M)
     }
 }
 
+// The DCT passes split into even and odd halves.  The DCT-II matrix
+// M[u][j] = 2 cos(pi (j + 1/2) u / K) (REDFT10) satisfies
+// M[u][K-1-j] = (-1)^u M[u][j], so the even outputs are sums over the
+// folded inputs x[j] + x[K-1-j] (and the middle input of an odd K) and the
+// odd outputs sums over the differences x[j] - x[K-1-j]: ceil(K/2) and
+// floor(K/2) terms instead of K.  The DCT-III matrix (REDFT01, [out][in])
+// satisfies M[K-1-i][u] = (-1)^u M[i][u], so outputs i and K-1-i are the
+// sum and the difference of the products over the even and the odd inputs.
+// Both use the first ceil(K/2) columns of the tables (fwd / inv) only, and
+// about half the multiply-adds of a full matrix pass; the results equal the
+// full passes' up to float rounding.
+template <int K>
+__device__ __forceinline__ void dct2_line(float (&v)[K], const float* M)
+{
+    constexpr int H = K / 2, NS = (K & 1) ? H + 1 : H;
+    float s[NS], d[H > 0 ? H : 1];
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+        s[j] = v[j] + v[K - 1 - j];
+        d[j] = v[j] - v[K - 1 - j];
+    }
+    if (K & 1) s[NS - 1] = v[H];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        float m = 0.f;
+        if ((u & 1) == 0) {
+#pragma unroll
+            for (int j = 0; j < NS; j++) m = __fmaf_rn(s[j], M[u * K + j], m);
+        } else {
+#pragma unroll
+            for (int j = 0; j < H; j++) m = __fmaf_rn(d[j], M[u * K + j], m);
+        }
+        v[u] = m;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void dct3_line(float (&v)[K], const float* M)
+{
+    constexpr int H = K / 2, NE = (K & 1) ? H + 1 : H;
+    float e[NE], o[H > 0 ? H : 1];
+#pragma unroll
+    for (int i = 0; i < NE; i++) {
+        float m = 0.f;
+#pragma unroll
+        for (int u = 0; u < K; u += 2) m = __fmaf_rn(v[u], M[i * K + u], m);
+        e[i] = m;
+    }
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+        float m = 0.f;
+#pragma unroll
+        for (int u = 1; u < K; u += 2) m = __fmaf_rn(v[u], M[i * K + u], m);
+        o[i] = m;
+    }
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+        v[i] = e[i] + o[i];
+        v[K - 1 - i] = e[i] - o[i];
+    }
+    if (K & 1) v[H] = e[NE - 1];
+}
+
+// x <- (line transform) along the rows (ROWS) or the columns of a K x K
+// block in registers.
+template <int K, bool ROWS, bool INV>
+__device__ __forceinline__ void dct_pass(float* x, const float* M)
+{
+#pragma unroll
+    for (int a = 0; a < K; a++) {
+        float v[K];
+#pragma unroll
+        for (int b = 0; b < K; b++) v[b] = ROWS ? x[a * K + b] : x[b * K + a];
+        if (INV) dct3_line<K>(v, M);
+        else dct2_line<K>(v, M);
+#pragma unroll
+        for (int b = 0; b < K; b++) {
+            if (ROWS) x[a * K + b] = v[b];
+            else x[b * K + a] = v[b];
+        }
+    }
+}
+
 // Forward 2D transform of slice g (stride-1 K*K floats in shared memory),
 // through registers, result back in g.
 template <int K, class TT>
@@ -161,8 +244,8 @@ __device__ __forceinline__ void slice_fwd2d(float* g, const StepHead& P, const T
             for (int j = 0; j < K; j++) g[i * K + j] = x[j * K + i];
     } else {
         // REDFT10 along rows then columns, then coef_norm (src/vbm3d.cpp:1294-1302)
-        row_pass<K, false>(x, T.fwd);
-        col_pass<K, false>(x, T.fwd);
+        dct_pass<K, true, false>(x, T.fwd);
+        dct_pass<K, false, false>(x, T.fwd);
 #pragma unroll
         for (int e = 0; e < K * K; e++) g[e] = x[e] * T.cn[e];
     }
@@ -188,8 +271,8 @@ __device__ __forceinline__ void slice_inv2d(float* g, const StepHead& P, const T
         // dct_2d_inv (src/vbm3d.cpp:1696-1709)
 #pragma unroll
         for (int e = 0; e < K * K; e++) x[e] = x[e] * T.cni[e];
-        row_pass<K, false>(x, T.inv);
-        col_pass<K, false>(x, T.inv);
+        dct_pass<K, true, true>(x, T.inv);
+        dct_pass<K, false, true>(x, T.inv);
         const float coef = 1.0f / (float)(K * 2);
 #pragma unroll
         for (int e = 0; e < K * K; e++) g[e] = coef * x[e];
@@ -227,7 +310,9 @@ __device__ __forceinline__ float col_dot(const float* xc, const float* M, int u)
 
 // Row pass of the owned rows (in place; optional elementwise scale of the
 // inputs first), and column pass of the owned columns into out[t][u].
-template <int K, int LPS, bool EXACT>
+// SPLIT: 0, the full matrix M (bior1.5 with EXACT); 1, the DCT-II and 2, the
+// DCT-III through their even / odd halves (dct2_line / dct3_line).
+template <int K, int LPS, bool EXACT, int SPLIT = 0>
 __device__ __forceinline__ void rows_owned(float* s, int part, const float* M, const float* pre)
 {
 #pragma unroll
@@ -237,13 +322,15 @@ __device__ __forceinline__ void rows_owned(float* s, int part, const float* M, c
         float xr[K], y[K];
 #pragma unroll
         for (int j = 0; j < K; j++) xr[j] = pre ? s[i * K + j] * pre[i * K + j] : s[i * K + j];
+        if (SPLIT == 1) dct2_line<K>(xr, M);
+        if (SPLIT == 2) dct3_line<K>(xr, M);
 #pragma unroll
-        for (int v = 0; v < K; v++) y[v] = row_dot<K, EXACT>(xr, M, v);
+        for (int v = 0; v < K; v++) y[v] = SPLIT ? xr[v] : row_dot<K, EXACT>(xr, M, v);
 #pragma unroll
         for (int v = 0; v < K; v++) s[i * K + v] = y[v];
     }
 }
-template <int K, int LPS, bool EXACT>
+template <int K, int LPS, bool EXACT, int SPLIT = 0>
 __device__ __forceinline__ void cols_owned(const float* s, int part, const float* M, float (&out)[(K + LPS - 1) / LPS][K])
 {
 #pragma unroll
@@ -253,8 +340,10 @@ __device__ __forceinline__ void cols_owned(const float* s, int part, const float
         float xc[K];
 #pragma unroll
         for (int i = 0; i < K; i++) xc[i] = s[i * K + j];
+        if (SPLIT == 1) dct2_line<K>(xc, M);
+        if (SPLIT == 2) dct3_line<K>(xc, M);
 #pragma unroll
-        for (int u = 0; u < K; u++) out[t][u] = col_dot<K, EXACT>(xc, M, u);
+        for (int u = 0; u < K; u++) out[t][u] = SPLIT ? xc[u] : col_dot<K, EXACT>(xc, M, u);
     }
 }
 
@@ -270,12 +359,12 @@ __device__ __forceinline__ void slices_fwd2d_shared(float* g, int nsl, int lane,
     float out[NL][K];
     if (act) {
         if (bior) rows_owned<K, LPS, true>(s, part, T.fwd, nullptr);
-        else rows_owned<K, LPS, false>(s, part, T.fwd, nullptr);
+        else rows_owned<K, LPS, false, 1>(s, part, T.fwd, nullptr);
     }
     __syncwarp();
     if (act) {
         if (bior) cols_owned<K, LPS, true>(s, part, T.fwd, out);
-        else cols_owned<K, LPS, false>(s, part, T.fwd, out);
+        else cols_owned<K, LPS, false, 1>(s, part, T.fwd, out);
     }
     __syncwarp();  // every column read before the (transposed) stores
     if (act) {
@@ -340,9 +429,9 @@ __device__ __forceinline__ void slices_inv2d_shared(float* g, int nsl, int lane,
             }
         }
     } else {
-        if (act) rows_owned<K, LPS, false>(s, part, T.inv, T.cni);
+        if (act) rows_owned<K, LPS, false, 2>(s, part, T.inv, T.cni);
         __syncwarp();
-        if (act) cols_owned<K, LPS, false>(s, part, T.inv, out);
+        if (act) cols_owned<K, LPS, false, 2>(s, part, T.inv, out);
         const float coef = 1.0f / (float)(K * 2);
         if (act) {
 #pragma unroll

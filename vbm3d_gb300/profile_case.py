@@ -1,11 +1,13 @@
 """One VBM3D run (both steps) on seeded synthetic data, for profilers.
 
-    python -m vbm3d_gb300.profile_case --width 1280 --height 720 --frames 16
+    python -m vbm3d_gb300.profile_case --width 1280 --height 720 --frames 16 [--runs 5]
     python -m vbm3d_gb300.profile_case --batch 64 [--scale 0.5]
     python -m vbm3d_gb300.profile_case --tvl1 --width 960 --height 540 --frames 16
 
 Plain form: one clip; launch order (colour transform on): color, bm (step
-1), filter<1>, normalize, bm (step 2), filter<2>, normalize, color x3.
+1), filter<1>, normalize, bm (step 2), filter<2>, normalize, color x3; with
+--runs > 1 it also prints the median time of a run (CUDA events, the first
+run left out).
 Batched form: the first `--batch` clips of the uneven-batch workload
 (synth.batch_specs, sides times `--scale`), one batch with a fixed
 configuration (no tuning pass), run once without the graph so that every
@@ -80,10 +82,21 @@ def main():
         return
     _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
     x0 = torch.from_numpy(noisy).cuda()
+    x = x0.clone()
+    times = []
     for _ in range(a.runs):
-        x = x0.clone()
+        x.copy_(x0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         vb.run(x, a.sigma, color_space=a.channels == 3)
-    torch.cuda.synchronize()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    if a.runs > 1:  # the first run pays the module loading and the memory pool's growth
+        ms = sorted(times[1:])[len(times[1:]) // 2]
+        print("plain %dx%dx%dx%d sigma %g: %.2f ms per run (median of %d), %.1f Mpix-frames/s"
+              % (a.width, a.height, a.frames, a.channels, a.sigma, ms, a.runs - 1,
+                 a.width * a.height * a.frames / 1e6 / (ms / 1e3)))
     print("ok")
 
 
