@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 import vbm3d_gb300 as vb
-from vbm3d_gb300.sure import mc_sure
+from vbm3d_gb300.sure import mc_sure, sure_step2_fixed_basic
 from vbm3d_gb300.synth import make_clip
 
 W, H, F, C, SIGMA = 480, 270, 16, 3, 25.0
@@ -70,6 +70,16 @@ def main():
                      "basic": {k: round(rb[k], 3) for k in ("mse", "sure_fd", "sure_linear")},
                      "final": {k: round(rf[k], 3) for k in ("mse", "sure_fd", "sure_linear")}})
     out["sure_sweep"] = rows
+    # step 2 with a fixed basic estimate: exact divergence of a linear map
+    _, noisy2, _, _ = make_clip(W, H, F, C, SIGMA, seed=5000 + 77)
+    y2 = vb.color_transform(torch.from_numpy(noisy2).to(dev), True)
+    b2 = vb.normalize(*vb.step1(y2, p1, SIGMA, color_space=True), y2)
+    fixed = []
+    for sf in (12.0, 18.0, 22.0, 25.0, 30.0, 40.0):
+        r = sure_step2_fixed_basic(y, SIGMA, sf, b2, clean=c, probes=2)
+        fixed.append({k: round(r[k], 3) for k in ("sigma_f", "mse", "sure", "sure_fd")})
+    out["sure_step2_fixed_basic"] = fixed
+    out["sure_step2_fixed_basic_max_rel_err"] = max(abs(r["sure"] - r["mse"]) / r["mse"] for r in fixed)
     for st in ("basic", "final"):
         mse = [r[st]["mse"] for r in rows]
         for kind in ("sure_fd", "sure_linear"):
