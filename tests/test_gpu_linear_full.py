@@ -109,8 +109,10 @@ def test_sure_exact_for_step2_with_fixed_basic(case, dev):
     from vbm3d_gb300.sure import sure_step2_fixed_basic
     clean = gpu(case["clean"], dev)
     y = gpu(case["noisy"], dev)
-    # the basic estimate from an independent noise realisation of the clip
-    _, noisy2, _, _ = make_clip(W, H, F, 3, SIGMA, 5000 + 77)
+    # the basic estimate from an independent noise realisation of the same
+    # clean clip (a stream of its own, so the pilot does not depend on y)
+    rng = np.random.default_rng(5077)
+    noisy2 = (case["clean"] + np.float32(SIGMA) * rng.standard_normal(case["clean"].shape, dtype=np.float32))
     y2 = vb.color_transform(gpu(noisy2, dev), True)
     basic = vb.normalize(*vb.step1(y2, vb.default_params(1, SIGMA), SIGMA, color_space=True), y2)
     rows = []

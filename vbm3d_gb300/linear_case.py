@@ -71,7 +71,8 @@ def main():
                      "final": {k: round(rf[k], 3) for k in ("mse", "sure_fd", "sure_linear")}})
     out["sure_sweep"] = rows
     # step 2 with a fixed basic estimate: exact divergence of a linear map
-    _, noisy2, _, _ = make_clip(W, H, F, C, SIGMA, seed=5000 + 77)
+    rng = np.random.default_rng(5077)  # an independent noise realisation of the same clean clip
+    noisy2 = (clean + np.float32(SIGMA) * rng.standard_normal(clean.shape, dtype=np.float32)).astype(np.float32)
     y2 = vb.color_transform(torch.from_numpy(noisy2).to(dev), True)
     b2 = vb.normalize(*vb.step1(y2, p1, SIGMA, color_space=True), y2)
     fixed = []
