@@ -10,11 +10,11 @@ RGB 480x270x16, AWGN sigma 25, colour transform on (YUV working space).
   * Monte-Carlo SURE where it is exact: step 2 with the basic estimate held
     fixed is the linear map L of its noisy input (groups and Wiener gains
     come from the basic estimate), so tr(L) estimated with Hutchinson
-    probes is its exact divergence and SURE is unbiased for its MSE.  The
-    basic estimate is computed from an independent noise realisation of the
-    same clean clip, so that it does not depend on the noisy input the
-    estimator is scored on; SURE must then track the true MSE over a sweep
-    of step 2's sigma.
+    probes is an unbiased estimate of its divergence and SURE is unbiased
+    for its MSE.  The basic estimate is computed from an independent noise
+    realisation of the same clean clip, so that it does not depend on the
+    noisy input the estimator is scored on; SURE must then track the true
+    MSE over a sweep of step 2's sigma and pick its minimiser.
 Each part prints one `LINEAR {...}` line with its figures.
 """
 import json
@@ -117,12 +117,17 @@ def test_sure_exact_for_step2_with_fixed_basic(case, dev):
     basic = vb.normalize(*vb.step1(y2, vb.default_params(1, SIGMA), SIGMA, color_space=True), y2)
     rows = []
     for sf in (12.0, 18.0, 22.0, 25.0, 30.0, 40.0):
-        r = sure_step2_fixed_basic(y, SIGMA, sf, basic, clean=clean, probes=2)
+        r = sure_step2_fixed_basic(y, SIGMA, sf, basic, clean=clean, probes=8)
         rows.append({k: r[k] for k in ("sigma_f", "mse", "sure", "sure_fd")})
     mse = np.array([r["mse"] for r in rows])
     sure = np.array([r["sure"] for r in rows])
     rel = np.abs(sure - mse) / mse
     print("LINEAR " + json.dumps(dict(check="SURE, step 2 with a fixed basic estimate", rows=rows,
                                       max_rel_err=float(rel.max()))))
-    assert rel.max() < 0.05, rows
+    # one noise realisation and 8 Hutchinson probes: SURE scatters around the
+    # true MSE by the probe error 2 sigma^2 (b^T J b - tr J) / n and the
+    # realisation's cross term 2 <noise, x - f> / n (together about 0.1 to
+    # 0.3 here, with MSE 3.4 to 13); it must follow the MSE and pick its
+    # minimiser
+    assert rel.max() < 0.10, rows
     assert int(np.argmin(sure)) == int(np.argmin(mse)), rows

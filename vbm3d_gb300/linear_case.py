@@ -77,10 +77,11 @@ def main():
     b2 = vb.normalize(*vb.step1(y2, p1, SIGMA, color_space=True), y2)
     fixed = []
     for sf in (12.0, 18.0, 22.0, 25.0, 30.0, 40.0):
-        r = sure_step2_fixed_basic(y, SIGMA, sf, b2, clean=c, probes=2)
+        r = sure_step2_fixed_basic(y, SIGMA, sf, b2, clean=c, probes=8)
         fixed.append({k: round(r[k], 3) for k in ("sigma_f", "mse", "sure", "sure_fd")})
     out["sure_step2_fixed_basic"] = fixed
     out["sure_step2_fixed_basic_max_rel_err"] = max(abs(r["sure"] - r["mse"]) / r["mse"] for r in fixed)
+    out["sure_step2_fixed_basic_argmin"] = [min(fixed, key=lambda r: r[k])["sigma_f"] for k in ("mse", "sure")]
     for st in ("basic", "final"):
         mse = [r[st]["mse"] for r in rows]
         for kind in ("sure_fd", "sure_linear"):
