@@ -80,6 +80,9 @@ def main():
         r = sure_step2_fixed_basic(y, SIGMA, sf, b2, clean=c, probes=8)
         fixed.append({k: round(r[k], 3) for k in ("sigma_f", "mse", "sure", "sure_fd")})
     out["sure_step2_fixed_basic"] = fixed
+    # the realisation's sample noise variance less sigma^2: the part of
+    # SURE - MSE common to every sigma_f
+    out["noise_variance_offset"] = float(np.mean((noisy.astype(np.float64) - clean) ** 2) - SIGMA ** 2)
     out["sure_step2_fixed_basic_max_rel_err"] = max(abs(r["sure"] - r["mse"]) / r["mse"] for r in fixed)
     out["sure_step2_fixed_basic_argmin"] = [min(fixed, key=lambda r: r[k])["sigma_f"] for k in ("mse", "sure")]
     for st in ("basic", "final"):
