@@ -46,6 +46,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--tvl1", action="store_true", help="TV-L1 flows of a one-channel clip")
     ap.add_argument("--ms", type=int, default=0, help="multiscaler DCT pyramid with this many levels")
+    ap.add_argument("--deterministic", action="store_true",
+                    help="plain form: the deterministic aggregation (vbm3d_set_deterministic)")
     ap.add_argument("--bm-tile", type=int, default=FIXED["bm1_tile"], help="batched block matching: refs per item")
     ap.add_argument("--bm-warps", type=int, default=FIXED["bm1_warps"], help="batched block matching: warps per block")
     a = ap.parse_args()
@@ -83,6 +85,7 @@ def main():
     _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
     x0 = torch.from_numpy(noisy).cuda()
     x = x0.clone()
+    vb.set_deterministic(a.deterministic)
     times = []
     for _ in range(a.runs):
         x.copy_(x0)
@@ -94,8 +97,9 @@ def main():
         times.append(e0.elapsed_time(e1))
     if a.runs > 1:  # the first run pays the module loading and the memory pool's growth
         ms = sorted(times[1:])[len(times[1:]) // 2]
-        print("plain %dx%dx%dx%d sigma %g: %.2f ms per run (median of %d), %.1f Mpix-frames/s"
-              % (a.width, a.height, a.frames, a.channels, a.sigma, ms, a.runs - 1,
+        print("plain%s %dx%dx%dx%d sigma %g: %.2f ms per run (median of %d), %.1f Mpix-frames/s"
+              % (" (deterministic)" if a.deterministic else "", a.width, a.height, a.frames, a.channels, a.sigma,
+                 ms, a.runs - 1,
                  a.width * a.height * a.frames / 1e6 / (ms / 1e3)))
     print("ok")
 
