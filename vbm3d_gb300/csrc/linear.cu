@@ -53,8 +53,10 @@ __device__ __forceinline__ void slice_fwd2d_T(float* g, const StepParams& P)
     } else {
 #pragma unroll
         for (int e = 0; e < K * K; e++) x[e] = x[e] * P.cn[e];
-        row_pass<K, false>(x, P.fwdT);
-        col_pass<K, false>(x, P.fwdT);
+        // the transposed DCT-II matrix has the DCT-III's output symmetry:
+        // its even / odd form (dct3_line) over the table fwdT
+        dct_pass<K, true, true>(x, P.fwdT);
+        dct_pass<K, false, true>(x, P.fwdT);
 #pragma unroll
         for (int e = 0; e < K * K; e++) g[e] = x[e];
     }
@@ -75,8 +77,9 @@ __device__ __forceinline__ void slice_inv2d_T(float* g, const StepParams& P)
 #pragma unroll
             for (int j = 0; j < K; j++) g[j * K + i] = x[i * K + j];
     } else {
-        row_pass<K, false>(x, P.invT);
-        col_pass<K, false>(x, P.invT);
+        // the transposed DCT-III matrix has the DCT-II's input symmetry
+        dct_pass<K, true, false>(x, P.invT);
+        dct_pass<K, false, false>(x, P.invT);
         const float coef = 1.0f / (float)(K * 2);
 #pragma unroll
         for (int e = 0; e < K * K; e++) g[e] = coef * x[e] * P.cni[e];
