@@ -9,8 +9,13 @@ namespace vbm3d {
 
 // ---------------------------------------------------------------- 1D ---
 
-// haar_forward / haar_inverse (src/lib_transforms.cpp:453-512).
-template <int N>
+// haar_forward / haar_inverse (src/lib_transforms.cpp:453-512).  EXACT:
+// the reference's (float)((double)s * SQRT2_INV) rounding (mul_sqrt2_inv),
+// which the hard-threshold step needs for its keep / zero decisions to be
+// the reference's; otherwise one float multiply by float(SQRT2_INV) (the
+// Wiener step, whose gains are continuous in the coefficients and whose
+// values differ from the reference's by float rounding anyway).
+template <int N, bool EXACT = true>
 __device__ __forceinline__ void haar_fwd(float* v)
 {
     float tmp[N > 1 ? N : 1];
@@ -18,15 +23,16 @@ __device__ __forceinline__ void haar_fwd(float* v)
     for (int k = N / 2; k >= 1; k /= 2) {
 #pragma unroll
         for (int i = 0; i < k; i++) {
-            tmp[i] = mul_sqrt2_inv(v[2 * i] + v[2 * i + 1]);
-            tmp[i + k] = mul_sqrt2_inv(v[2 * i] - v[2 * i + 1]);
+            const float a = v[2 * i] + v[2 * i + 1], b = v[2 * i] - v[2 * i + 1];
+            tmp[i] = EXACT ? mul_sqrt2_inv(a) : a * kS2iHi;
+            tmp[i + k] = EXACT ? mul_sqrt2_inv(b) : b * kS2iHi;
         }
 #pragma unroll
         for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
     }
 }
 
-template <int N>
+template <int N, bool EXACT = true>
 __device__ __forceinline__ void haar_inv(float* v)
 {
     float tmp[N > 1 ? N : 1];
@@ -34,8 +40,9 @@ __device__ __forceinline__ void haar_inv(float* v)
     for (int k = 1; k * 2 <= N; k *= 2) {
 #pragma unroll
         for (int i = 0; i < k; i++) {
-            tmp[2 * i] = mul_sqrt2_inv(v[i] + v[i + k]);
-            tmp[2 * i + 1] = mul_sqrt2_inv(v[i] - v[i + k]);
+            const float a = v[i] + v[i + k], b = v[i] - v[i + k];
+            tmp[2 * i] = EXACT ? mul_sqrt2_inv(a) : a * kS2iHi;
+            tmp[2 * i + 1] = EXACT ? mul_sqrt2_inv(b) : b * kS2iHi;
         }
 #pragma unroll
         for (int i = 0; i < 2 * k; i++) v[i] = tmp[i];
@@ -533,16 +540,16 @@ __device__ __forceinline__ float wiener_vector(const float* gn, float* gb, int s
         }
         hadamard<N>(vb);
     } else {
-        haar_fwd<N>(vn);
-        haar_fwd<N>(vb);
+        haar_fwd<N, false>(vn);
+        haar_fwd<N, false>(vb);
 #pragma unroll
         for (int n = 0; n < N; n++) {
             float value = vb[n] * vb[n];
-            value = value / (value + s2);
+            value = __fdividef(value, value + s2);  // a gain in [0, 1): 2-ulp quotient
             vb[n] = vn[n] * value;
             wsum = wsum + value * value;
         }
-        haar_inv<N>(vb);
+        haar_inv<N, false>(vb);
     }
 #pragma unroll
     for (int n = 0; n < N; n++) gb[n * stride] = vb[n];
