@@ -17,8 +17,9 @@
 //     collects the entries of every patch position that covers the
 //     segment (k rows of contiguous bucket ranges), sorts them by the key
 //     r * 8 + n in shared memory (bitonic) and walks them in that order,
-//     each lane adding the terms of the entries that cover its pixel, for
-//     every channel.  Segments with more entries than a warp holds go to
+//     32 at a time: each entry's mask of covered pixels, bit-transposed,
+//     gives every lane the entries that cover its pixel, and the lane adds
+//     their terms in key order, for every channel.  Segments with more entries than a warp holds go to
 //     det_gather_big (a block sorts up to 16384; beyond that each lane
 //     selects its entries in key order by repeated minimum search).
 //
@@ -254,6 +255,46 @@ __device__ __forceinline__ void add_entry(const StepHead& P, const KaiserTable& 
     }
 }
 
+// Column `lane` of the 32 x 32 bit matrix whose row r lane r holds in x:
+// bit r of the result is bit `lane` of lane r's x (five exchange rounds of
+// the off-diagonal blocks).
+__device__ __forceinline__ unsigned transpose_round(unsigned x, int lane, int j, unsigned hi)
+{
+    const unsigned y = __shfl_xor_sync(kFull, x, j);
+    return (lane & j) ? ((x & hi) | ((y & hi) >> j)) : ((x & ~hi) | ((y & ~hi) << j));
+}
+__device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
+{
+    x = transpose_round(x, lane, 16, 0xFFFF0000u);
+    x = transpose_round(x, lane, 8, 0xFF00FF00u);
+    x = transpose_round(x, lane, 4, 0xF0F0F0F0u);
+    x = transpose_round(x, lane, 2, 0xCCCCCCCCu);
+    return transpose_round(x, lane, 1, 0xAAAAAAAAu);
+}
+
+// The sorted entries list[0 .. T) of segment s, added at the pixels they
+// cover: a warp takes them 32 at a time; each lane's entry gives a mask of
+// the lanes (pixels) its patch covers, the transposed masks give each lane
+// the entries of the chunk that cover its pixel, which it adds in key
+// order.  Every lane of the warp calls it.
+template <int K>
+__device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable& kt, const uint2* list, unsigned T,
+                                            const Seg& s, int lane, const float* __restrict__ est,
+                                            const float* __restrict__ wts, float (&num)[kMaxC], float (&den)[kMaxC])
+{
+    const int x = s.x0 + lane;
+    for (unsigned c0 = 0; c0 < T; c0 += 32) {
+        unsigned m = 0;
+        if (c0 + lane < T) {
+            const int lo = (int)(list[c0 + lane].y & 0xffffu) - s.x0;  // first covered lane (may be < 0)
+            const int a = max(lo, 0), b = min(lo + K, 32);
+            if (b > a) m = (b - a == 32 ? 0xffffffffu : ((1u << (b - a)) - 1u)) << a;
+        }
+        for (unsigned mine = transpose32(m, lane); mine; mine &= mine - 1)
+            add_entry<K>(P, kt, list[c0 + (unsigned)(__ffs(mine) - 1)], x, s.y, est, wts, num, den);
+    }
+}
+
 template <int K>
 __device__ __forceinline__ void seg_write(const StepHead& P, const Seg& s, int x, const float (&num)[kMaxC],
                                           const float (&den)[kMaxC], float* __restrict__ pair)
@@ -297,7 +338,7 @@ det_gather(const StepHead P, const KaiserTable kt, const float* __restrict__ est
         }
     float num[kMaxC] = {0.f, 0.f, 0.f}, den[kMaxC] = {0.f, 0.f, 0.f};
     const int x = s.x0 + lane;
-    for (unsigned i = 0; i < T; i++) add_entry<K>(P, kt, list[i], x, s.y, est, wts, num, den);
+    walk_sorted<K>(P, kt, list, T, s, lane, est, wts, num, den);
     seg_write<K>(P, s, x, num, den, pair);
 }
 
@@ -330,7 +371,7 @@ det_gather_big(const StepHead P, const KaiserTable kt, const float* __restrict__
                     __syncthreads();
                 }
             if (threadIdx.x < 32) {
-                for (unsigned i = 0; i < T; i++) add_entry<K>(P, kt, blist[i], x, s.y, est, wts, num, den);
+                walk_sorted<K>(P, kt, blist, T, s, lane, est, wts, num, den);
                 seg_write<K>(P, s, x, num, den, pair);
             }
             __syncthreads();
