@@ -182,7 +182,10 @@ int vbm3d_gpu_run(float sigma, float *noisy, const float *fflow, const float *bf
 /* vbm3d_gpu_run on HOST buffers: copies noisy (and flows, when not NULL) to
  * the device, runs both passes, copies basic and denoised back, and waits.
  * `noisy` is not modified (the reference converts its copy back to RGB).
- * This is the call a CPU program that used run_vbm3d makes. */
+ * This is the call a CPU program that used run_vbm3d makes.  Host flows
+ * need only F - 1 frames (the frames the reference's flow files hold,
+ * src/main.cpp:360, :369): the steps never read the last one, and only the
+ * first F - 1 are copied. */
 int vbm3d_run_host(float sigma, const float *noisy, const float *fflow, const float *bflow,
                    float *basic, float *denoised,
                    const vbm3d_params *prms_1, const vbm3d_params *prms_2,
@@ -191,7 +194,8 @@ int vbm3d_run_host(float sigma, const float *noisy, const float *fflow, const fl
 /* One step on HOST buffers (copies in, runs vbm3d_gpu_step1 or _step2,
  * copies numerator and denominator out, waits): the call a CPU caller of
  * vbm3d_1st_step / vbm3d_2nd_step (src/vbm3d.h:38-70) makes.  `step` is 1
- * or 2; `basic` is read for step 2 only. */
+ * or 2; `basic` is read for step 2 only.  Host flows need only F - 1
+ * frames, as for vbm3d_run_host. */
 int vbm3d_step_host(int step, const vbm3d_params *prms, const float *noisy, const float *basic,
                     const float *fflow, const float *bflow, vbm3d_dims dims,
                     float sigma, int color_space, float *numerator, float *denominator);

@@ -83,3 +83,22 @@ def test_steps_with_file_flows_match_the_c_abi(exe, tmp_path, clip):
     assert rc == 0, err
     o2n, o2d = o.step(2, o.default_params(2, 25.0), 25.0, yuv, basic, ff, bf, True)
     assert np.abs(ratio(num2, den2, basic) - ratio(o2n, o2d, basic)).max() <= TOL
+
+
+def test_host_entry_points_take_f_minus_1_frame_flows(clip):
+    # vbm3d_run_host / vbm3d_step_host copy only a flow's first F - 1 frames
+    # (the steps never read the last): F - 1-frame host flows give the same
+    # bits as F-frame ones (deterministic aggregation, so runs compare bit
+    # for bit)
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    _, noisy, ff, bf = clip
+    F = noisy.shape[0]
+    with vb.Deterministic(True):
+        a = vb.run_host(noisy, 25.0, fflow=ff, bflow=bf, color_space=True)
+        b = vb.run_host(noisy, 25.0, fflow=np.ascontiguousarray(ff[:F - 1]), bflow=np.ascontiguousarray(bf[:F - 1]),
+                        color_space=True)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+    with pytest.raises(ValueError):
+        vb.run_host(noisy, 25.0, fflow=np.ascontiguousarray(ff[:F - 2]), color_space=True)

@@ -479,9 +479,16 @@ def run(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=Fals
 
 
 def run_host(noisy, sigma, p1=None, p2=None, fflow=None, bflow=None, color_space=False, basic=None, out=None):
-    """run_vbm3d on host (numpy) arrays: copies in, denoises, copies out."""
+    """run_vbm3d on host (numpy) arrays: copies in, denoises, copies out.
+    Flows [frames, 2, H, W] with F or F - 1 frames (the last is never read)."""
     import numpy as np
     noisy = np.ascontiguousarray(noisy, dtype=np.float32)
+    F, _, H, W = noisy.shape
+    for name, fl in (("fflow", fflow), ("bflow", bflow)):
+        if fl is not None and (fl.dtype != np.float32 or not fl.flags.c_contiguous or fl.shape[1:] != (2, H, W)
+                               or fl.shape[0] not in (F, F - 1)):
+            raise ValueError("%s: float32 C-contiguous [F or F - 1, 2, %d, %d] expected, got %s %s"
+                             % (name, H, W, fl.dtype, fl.shape))
     p1 = default_params(1, sigma) if p1 is None else p1
     p2 = default_params(2, sigma) if p2 is None else p2
     basic = np.empty_like(noisy) if basic is None else basic

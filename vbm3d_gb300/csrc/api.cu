@@ -403,6 +403,21 @@ int run_step(int step, const vbm3d_params* prms, const float* noisy, const float
     return rc;
 }
 
+// A host flow onto the device: the steps never read a flow's last frame
+// (forward chains stop at the last frame, backward chains and trajectories
+// read frames up to F - 2), so only the first F - 1 frames are copied, and
+// a caller may pass the F - 1 frames its flow files hold; the device copy's
+// last frame is zeroed.
+cudaError_t upload_flow(float* d, const float* h, vbm3d_dims dims, cudaStream_t s)
+{
+    const size_t frame = (size_t)dims.width * dims.height * 2;
+    const size_t used = frame * (dims.frames - 1);
+    cudaError_t e = cudaSuccess;
+    if (used) e = cudaMemcpyAsync(d, h, used * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + used, 0, frame * sizeof(float), s);
+    return e;
+}
+
 }  // namespace
 
 namespace vbm3d {
@@ -659,8 +674,8 @@ int vbm3d_step_host(int step, const vbm3d_params* prms, const float* noisy, cons
     if (e == cudaSuccess && bflow) e = pool_alloc(&d_bf, nf, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_noisy, noisy, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && step == 2) e = cudaMemcpyAsync(d_basic, basic, n * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && fflow) e = cudaMemcpyAsync(d_ff, fflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && bflow) e = cudaMemcpyAsync(d_bf, bflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && fflow) e = upload_flow(d_ff, fflow, dims, s);
+    if (e == cudaSuccess && bflow) e = upload_flow(d_bf, bflow, dims, s);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "device buffers");
     } else {
@@ -697,8 +712,8 @@ int vbm3d_run_host(float sigma, const float* noisy, const float* fflow, const fl
     if (e == cudaSuccess && fflow) e = pool_alloc(&d_ff, nf, s);
     if (e == cudaSuccess && bflow) e = pool_alloc(&d_bf, nf, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_noisy, noisy, n * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && fflow) e = cudaMemcpyAsync(d_ff, fflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && bflow) e = cudaMemcpyAsync(d_bf, bflow, nf * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && fflow) e = upload_flow(d_ff, fflow, dims, s);
+    if (e == cudaSuccess && bflow) e = upload_flow(d_bf, bflow, dims, s);
     if (e == cudaSuccess && prms_1 && prms_1->k == 0)
         e = cudaMemcpyAsync(d_basic, basic, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) {

@@ -21,15 +21,13 @@
 // from flow files: fflow of frames first..last-1, bflow of first+1..last,
 // src/main.cpp:360, :369).  The steps never read a flow's frame F - 1
 // (forward chains stop at the last frame, backward chains read bflow[t - 1]),
-// so an F - 1-frame flow is passed as an F-frame buffer whose last frame is
-// zero.  Any other size is the mismatch main.cpp rejects
+// and the host entry points copy only the first F - 1 frames, so both are
+// passed as they are.  Any other size is the mismatch main.cpp rejects
 // (src/main.cpp:372-376): VBM3D_ERR_SIZE_MISMATCH.
-#include <algorithm>
 #include <cassert>
 #include <cstdio>
 #include <cstdlib>
 #include <ctime>  // the reference headers use time() and assert() without including them
-#include <vector>
 
 #include "vbm3d.h"
 #include "vbm3d_gb300.h"
@@ -54,33 +52,26 @@ vbm3d_dims dims_of(const Video<float>& v)
     return d;
 }
 
-// The flow buffer the C ABI reads (W*H*F*2 floats, or NULL for zero flow)
-// for flow f of video vid; `pad` holds the zero-padded copy of an
-// F - 1-frame flow.  Returns VBM3D_OK or VBM3D_ERR_SIZE_MISMATCH.
-int flow_arg(const Video<float>& f, const Video<float>& vid, std::vector<float>& pad, const float** out)
+// The flow the C ABI reads (its first F - 1 frames; NULL for zero flow) for
+// flow f of video vid.  Returns VBM3D_OK or VBM3D_ERR_SIZE_MISMATCH.
+int flow_arg(const Video<float>& f, const Video<float>& vid, const float** out)
 {
     *out = NULL;
     if (f.sz.whcf == 0) return VBM3D_OK;
     if (f.sz.width != vid.sz.width || f.sz.height != vid.sz.height || f.sz.channels != 2)
         return VBM3D_ERR_SIZE_MISMATCH;
-    if (f.sz.frames == vid.sz.frames) {
-        *out = f.data.data();
-        return VBM3D_OK;
-    }
-    if (f.sz.frames + 1 != vid.sz.frames) return VBM3D_ERR_SIZE_MISMATCH;
-    pad.assign((size_t)vid.sz.wh * 2 * vid.sz.frames, 0.f);
-    std::copy(f.data.begin(), f.data.begin() + (size_t)f.sz.whcf, pad.begin());
-    *out = pad.data();
+    if (f.sz.frames != vid.sz.frames && f.sz.frames + 1 != vid.sz.frames) return VBM3D_ERR_SIZE_MISMATCH;
+    *out = f.data.data();
     return VBM3D_OK;
 }
 
 // Both flows of a call; prints the reason and returns the status on a
 // mismatch.
-int flow_args(const Video<float>& ff, const Video<float>& bf, const Video<float>& vid, std::vector<float>& fpad,
-              std::vector<float>& bpad, const float** fp, const float** bp)
+int flow_args(const Video<float>& ff, const Video<float>& bf, const Video<float>& vid, const float** fp,
+              const float** bp)
 {
-    int rc = flow_arg(ff, vid, fpad, fp);
-    if (rc == VBM3D_OK) rc = flow_arg(bf, vid, bpad, bp);
+    int rc = flow_arg(ff, vid, fp);
+    if (rc == VBM3D_OK) rc = flow_arg(bf, vid, bp);
     if (rc != VBM3D_OK)
         std::fprintf(stderr, "vbm3d_gb300: %s: flows of %ux%ux%u(x%u) / %ux%ux%u(x%u) for a %ux%ux%u video\n",
                      vbm3d_status_string(rc), ff.sz.width, ff.sz.height, ff.sz.frames, ff.sz.channels, bf.sz.width,
@@ -99,9 +90,8 @@ void step(int which, const float sigma, const Video<float>& noisy, const Video<f
         return;
     }
     vbm3d_params p = to_c(prms);
-    std::vector<float> fpad, bpad;
     const float *fp = NULL, *bp = NULL;
-    int rc = flow_args(fflow, bflow, noisy, fpad, bpad, &fp, &bp);
+    int rc = flow_args(fflow, bflow, noisy, &fp, &bp);
     if (rc == VBM3D_OK) {
         rc = vbm3d_step_host(which, &p, noisy.data.data(), basic ? basic->data.data() : NULL, fp, bp,
                              dims_of(noisy), sigma, color_space ? 1 : 0, num.data.data(), den.data.data());
@@ -136,9 +126,8 @@ int run_vbm3d(const float sigma, Video<float>& vid_noisy, Video<float>& fflow, V
     if (vid_basic.sz != vid_noisy.sz) vid_basic.resize(vid_noisy.sz);
     if (vid_denoised.sz != vid_noisy.sz) vid_denoised.resize(vid_noisy.sz);
     vbm3d_params p1 = to_c(prms_1), p2 = to_c(prms_2);
-    std::vector<float> fpad, bpad;
     const float *fp = NULL, *bp = NULL;
-    if (flow_args(fflow, bflow, vid_noisy, fpad, bpad, &fp, &bp) != VBM3D_OK) return EXIT_FAILURE;
+    if (flow_args(fflow, bflow, vid_noisy, &fp, &bp) != VBM3D_OK) return EXIT_FAILURE;
     int rc = vbm3d_run_host(sigma, vid_noisy.data.data(), fp, bp, vid_basic.data.data(), vid_denoised.data.data(),
                             &p1, &p2, color_space ? 1 : 0, dims_of(vid_noisy));
     if (rc != VBM3D_OK) {
