@@ -12,7 +12,7 @@ struct Layout {
     int warp_bytes;   // shared memory per warp
     int tile_floats;  // staged windows
     int res_cap;      // distances of a phase / the final list
-    int scr_cap;      // tie fallback scratch (one window)
+    int scr_cap;      // tie fallback scratch (one window), inside the tile area
 };
 
 namespace {
@@ -701,8 +701,9 @@ __device__ __forceinline__ void bm2_ref(const StepHead& P, const Layout& L, long
     off = align16(off + sizeof(float) * L.tile_floats);
     S.res = reinterpret_cast<Pair*>(ws + off);
     off = align16(off + sizeof(Pair) * L.res_cap);
-    S.scr = reinterpret_cast<Pair*>(ws + off);
-    off = align16(off + sizeof(Pair) * L.scr_cap);
+    // the tie fallback's scratch shares the tile area: ties are sorted after
+    // a phase's distances, and the next phase stages its tiles afterwards
+    S.scr = reinterpret_cast<Pair*>(S.tiles);
     S.fc = reinterpret_cast<Pair*>(ws + off);
     off = align16(off + sizeof(Pair) * 2 * Nb * Nb);
     S.best = reinterpret_cast<Pair*>(ws + off);
@@ -895,15 +896,16 @@ inline Layout bm2_layout(const StepHead& P)
     const int p0 = bm2_pitch(P.Ns, P.k), p1 = bm2_pitch(P.Npr, P.k);
     // phase 0: one Ns window; phase f: up to 2 Nb Npr windows in pairs; plus
     // the one-column over-read of the last slot of an odd-width window
-    L.tile_floats = max(P.C * p0 * (P.Ns + P.k - 1), P.Nb * bm2_pair_stride(P.C * p1 * (P.Npr + P.k - 1))) + 8;
+    L.scr_cap = max(P.Ns * P.Ns, P.Npr * P.Npr);
+    // (the tile area also holds the tie fallback's scratch of scr_cap pairs)
+    L.tile_floats = max(max(P.C * p0 * (P.Ns + P.k - 1), P.Nb * bm2_pair_stride(P.C * p1 * (P.Npr + P.k - 1))) + 8,
+                        2 * L.scr_cap);
     L.tile_floats = (L.tile_floats + 3) & ~3;
     L.res_cap = max(max(P.Ns * P.Ns, 2 * P.Nb * P.Npr * P.Npr), P.Nb * (1 + 2 * P.Nf));
-    L.scr_cap = max(P.Ns * P.Ns, P.Npr * P.Npr);
     // the same sequence of 16-byte aligned regions as the kernel
     size_t off = align16(sizeof(float2) * P.C * P.k * bm2_ref_row(P.k));
     off = align16(off + sizeof(float) * L.tile_floats);
     off = align16(off + sizeof(Pair) * L.res_cap);
-    off = align16(off + sizeof(Pair) * L.scr_cap);
     off = align16(off + sizeof(Pair) * 2 * P.Nb * P.Nb);
     off = align16(off + sizeof(Pair) * P.bm_best_cap);
     off = align16(off + sizeof(Win) * P.bm_win_cap);
