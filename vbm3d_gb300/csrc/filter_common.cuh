@@ -693,13 +693,35 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
         }
         return;
     }
-    const size_t W = (size_t)P.W, wh = (size_t)P.wh;
-    for (int e = lane; e < total; e += 32) {
-        const int sl = e / K2, pq = e - sl * K2;
-        const int c = sl >> log2n, n = sl & (nsx - 1);
-        const int p = pq / K, q = pq - p * K;
-        const float kw = T.kaiser[pq] * wgt[c];
-        agg_add<PAIR>(A, idx[n] + (size_t)c * wh + (size_t)p * W + q, kw * ge[sl * SS + pq], kw);
+    // lanes over the pixels of a patch, the group's slices in the inner
+    // loops: a lane's pixel offset and Kaiser weight are set once, the
+    // slice's channel weight and patch index are the same on every lane.
+    // Offsets within a clip fit 32 bits (W * H * F * C < 2^32).
+    (void)total;
+    constexpr int NG = 8;  // group sizes of this body (N <= 8, as group_1d)
+    unsigned pos[NG];
+#pragma unroll
+    for (int n = 0; n < NG; n++) pos[n] = n < nsx ? idx[n] : 0u;
+    const unsigned W = (unsigned)P.W, wh = (unsigned)P.wh;
+#pragma unroll
+    for (int pq0 = 0; pq0 < K2; pq0 += 32) {
+        const int pq = pq0 + lane;
+        if (pq < K2) {
+            const int p = pq / K, q = pq - p * K;
+            const unsigned off = (unsigned)p * W + (unsigned)q;
+            const float kai = T.kaiser[pq];
+#pragma unroll
+            for (int c = 0; c < kMaxC; c++) {
+                if (c < C) {
+                    const float kw = kai * wgt[c];
+                    const float* gc = ge + (c << log2n) * SS + pq;
+                    const unsigned oc = (unsigned)c * wh + off;
+#pragma unroll
+                    for (int n = 0; n < NG; n++)
+                        if (n < nsx) agg_add<PAIR>(A, (size_t)(pos[n] + oc), kw * gc[n * SS], kw);
+                }
+            }
+        }
     }
 }
 
