@@ -464,16 +464,34 @@ template <int K, int SS>
 __device__ __forceinline__ void gather_k(const StepHead& P, const float* __restrict__ vid, const unsigned* idx,
                                          int nsx, int log2n, float* g, int lane)
 {
-    constexpr int K2 = K * K;
-    // geometry in registers before the first copy (cp_async4s)
-    const int total = P.C * nsx * K2;
-    const long long W = P.W, wh = P.wh;
+    constexpr int K2 = K * K, NG = 8;  // group sizes up to 8
+    // lanes over the pixels of a patch, the group's slices in unrolled inner
+    // loops: a lane's pixel offset is set once, the patch positions and the
+    // clip's geometry are in registers before the first copy (cp_async4s);
+    // offsets within a clip fit 32 bits (W * H * F * C < 2^32)
+    unsigned pos[NG];
+#pragma unroll
+    for (int n = 0; n < NG; n++) pos[n] = n < nsx ? idx[n] : 0u;
+    const unsigned W = (unsigned)P.W, wh = (unsigned)P.wh;
+    const int C = P.C;
     const unsigned g0 = smem_addr(g);
-    for (int e = lane; e < total; e += 32) {
-        const int sl = e / K2, pq = e - sl * K2;
-        const int c = sl >> log2n, n = sl & (nsx - 1);
-        const int p = pq / K, q = pq - p * K;
-        cp_async4s(g0 + 4u * (unsigned)(sl * SS + pq), vid + idx[n] + c * wh + p * W + q);
+#pragma unroll
+    for (int pq0 = 0; pq0 < K2; pq0 += 32) {
+        const int pq = pq0 + lane;
+        if (pq < K2) {
+            const int p = pq / K, q = pq - p * K;
+            const unsigned off = (unsigned)p * W + (unsigned)q;
+#pragma unroll
+            for (int c = 0; c < kMaxC; c++) {
+                if (c < C) {
+                    const unsigned oc = (unsigned)c * wh + off;
+                    const unsigned dc = g0 + 4u * (unsigned)((c << log2n) * SS + pq);
+#pragma unroll
+                    for (int n = 0; n < NG; n++)
+                        if (n < nsx) cp_async4s(dc + 4u * (unsigned)(n * SS), vid + (pos[n] + oc));
+                }
+            }
+        }
     }
 }
 
@@ -559,17 +577,18 @@ __device__ __forceinline__ float wiener_vector(const float* gn, float* gb, int s
 // 1D transform along the group, shrinkage and the per-channel weights of
 // one group held in shared memory as slices [c][n][k*k] of stride ss; one
 // coefficient vector (c, pq) per lane.
-template <int STEP, int NMAX = 32>
+template <int STEP, int NMAX = 32, int K = 0>
 __device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB, int nsx, int ss, int lane,
                                         float* wgt)
 {
     // slices are laid out [c][n][ht][k*k] with stride ss; the coefficient
     // vector (c, ht, pq) runs over n with stride kt*ss.  Its index in the
     // reference's group_3D is pq + ht*k*k, so the group DC is pq = ht = 0.
-    const int k2 = P.k * P.k, kt = P.kt, k2t = k2 * kt, C = P.C, ns = kt * ss;
+    // K > 0: the register-resident path's compile-time k (kt == 1)
+    const int k2 = K ? K * K : P.k * P.k, kt = K ? 1 : P.kt, k2t = k2 * kt, C = P.C, ns = kt * ss;
     float acc[kMaxC] = {0.f, 0.f, 0.f};
     for (int v = lane; v < C * k2t; v += 32) {
-        const int c = v / k2t, rem = v - c * k2t, ht = rem / k2, pq = rem - ht * k2;
+        const int c = v / k2t, rem = v - c * k2t, ht = K ? 0 : rem / k2, pq = rem - ht * k2;
         float* ga = gA + ((size_t)(c * nsx) * kt + ht) * ss + pq;
         float* gb = gB + ((size_t)(c * nsx) * kt + ht) * ss + pq;
         const bool dc = pq == 0 && ht == 0;
@@ -584,7 +603,9 @@ __device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB
                 case 16: kept = ht_vector<(NMAX < 16 ? NMAX : 16)>(ga, ns, dc, T, P.T3D); break;
                 default: kept = ht_vector<NMAX>(ga, ns, dc, T, P.T3D); break;
             }
-            acc[c] += (float)kept;
+#pragma unroll
+            for (int cc = 0; cc < kMaxC; cc++)
+                if (cc == c) acc[cc] += (float)kept;
         } else {
             const float s2 = P.sigma[c] * P.sigma[c];
             float ws;
@@ -596,7 +617,9 @@ __device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB
                 case 16: ws = wiener_vector<(NMAX < 16 ? NMAX : 16)>(ga, gb, ns, s2, P.T3D); break;
                 default: ws = wiener_vector<NMAX>(ga, gb, ns, s2, P.T3D); break;
             }
-            acc[c] += ws;
+#pragma unroll
+            for (int cc = 0; cc < kMaxC; cc++)
+                if (cc == c) acc[cc] += ws;
         }
     }
 #pragma unroll
@@ -663,7 +686,7 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
     }
 
     float wgt[kMaxC];
-    group_1d<STEP, 8>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
+    group_1d<STEP, 8, K>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
 
     // inverse 2D, as the forward one
     float* ge = STEP == 1 ? gA : gB;
