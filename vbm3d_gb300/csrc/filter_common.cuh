@@ -584,8 +584,11 @@ __device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB
     // slices are laid out [c][n][ht][k*k] with stride ss; the coefficient
     // vector (c, ht, pq) runs over n with stride kt*ss.  Its index in the
     // reference's group_3D is pq + ht*k*k, so the group DC is pq = ht = 0.
-    // K > 0: the register-resident path's compile-time k (kt == 1)
-    const int k2 = K ? K * K : P.k * P.k, kt = K ? 1 : P.kt, k2t = k2 * kt, C = P.C, ns = kt * ss;
+    // K > 0: the register-resident path's compile-time k (kt == 1, slice
+    // stride (k*k) | 1 as filter_ref lays the slices out)
+    const int k2 = K ? K * K : P.k * P.k, kt = K ? 1 : P.kt, k2t = k2 * kt, C = P.C;
+    const int ns = K ? ((K * K) | 1) : kt * ss;
+    if (K) ss = ns;
     float acc[kMaxC] = {0.f, 0.f, 0.f};
     for (int v = lane; v < C * k2t; v += 32) {
         const int c = v / k2t, rem = v - c * k2t, ht = K ? 0 : rem / k2, pq = rem - ht * k2;
@@ -697,17 +700,31 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
         __syncwarp();
     }
 
-    // aggregation (src/vbm3d.cpp:612-650), lanes over consecutive pixels
-    const int total = nsl * K2;
+    // aggregation (src/vbm3d.cpp:612-650)
+    constexpr int NG = 8;  // group sizes of this body (N <= 8, as group_1d)
     if (STORE) {
         // the products the reference adds, kept for the ordered second pass:
         // est[r][c][n][pq] = (kaiser[pq] * w_c) * est, the reference's
-        // evaluation order of kai * w * e (src/vbm3d.cpp:641-643)
+        // evaluation order of kai * w * e (src/vbm3d.cpp:641-643); lanes
+        // over the pixels of a patch, as below
         float* er = A.est + (size_t)r * (size_t)(C * P.N * K2);
-        for (int e = lane; e < total; e += 32) {
-            const int sl = e / K2, pq = e - sl * K2;
-            const int c = sl >> log2n, n = sl & (nsx - 1);
-            er[((size_t)c * P.N + n) * K2 + pq] = (T.kaiser[pq] * wgt[c]) * ge[sl * SS + pq];
+#pragma unroll
+        for (int pq0 = 0; pq0 < K2; pq0 += 32) {
+            const int pq = pq0 + lane;
+            if (pq < K2) {
+                const float kai = T.kaiser[pq];
+#pragma unroll
+                for (int c = 0; c < kMaxC; c++) {
+                    if (c < C) {
+                        const float kw = kai * wgt[c];
+                        const float* gc = ge + (c << log2n) * SS + pq;
+                        float* ec = er + c * P.N * K2 + pq;
+#pragma unroll
+                        for (int n = 0; n < NG; n++)
+                            if (n < nsx) ec[n * K2] = kw * gc[n * SS];
+                    }
+                }
+            }
         }
         if (lane == 0) {
 #pragma unroll
@@ -720,8 +737,6 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
     // loops: a lane's pixel offset and Kaiser weight are set once, the
     // slice's channel weight and patch index are the same on every lane.
     // Offsets within a clip fit 32 bits (W * H * F * C < 2^32).
-    (void)total;
-    constexpr int NG = 8;  // group sizes of this body (N <= 8, as group_1d)
     unsigned pos[NG];
 #pragma unroll
     for (int n = 0; n < NG; n++) pos[n] = n < nsx ? idx[n] : 0u;
