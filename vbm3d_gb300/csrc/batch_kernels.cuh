@@ -41,12 +41,12 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // plain kernel does.  Block matching reads its clips' parameters from the
 // launch's kernel-argument table (batch.cuh).  Filtering keeps its current
 // clip's scalar parameters in shared memory, reloaded when an item of
-// another clip comes up; for k = 8 it reads the transform tables of its
-// class (the same for every clip of the launch) from its kernel arguments,
-// so each table entry is a constant-bank operand of the transforms' FMAs
-// (-7 % to -16 % per launch), while for k = 7 that form needs more than its
-// 128 registers and spills (+25 % to +40 %), so k = 7 reads the tables from
-// the shared-memory copy.
+// another clip comes up, and reads the transform tables of its class (the
+// same for every clip of the launch) from its kernel arguments, so each
+// table entry is a constant-bank operand of the transforms' FMAs (k = 8:
+// -7 % to -16 % per launch against tables in shared memory; k = 7, with
+// the DCT passes through their even and odd halves: 96 registers instead
+// of 128, step-2 RGB launches -3.5 % to -7 %).
 
 // A reference patch takes a group of G lanes, as in bm2_kernel: a warp for
 // three channels, a half warp for one.
@@ -95,19 +95,14 @@ batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict
         claim_item(items, nitems, head, &s_item[buf ^ 1]);
         const BatchClip& B = clips[I.x];
         if (I.x != cur) {
-            if (K == 8) copy_words(&V->h, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
-            else copy_words(V, &B.s[STEP - 1].v, (int)sizeof(FilterView));
+            copy_words(&V->h, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
             __syncthreads();
             cur = I.x;
         }
         const AggTarget A{nullptr, nullptr, B.pair};
         for (unsigned j = wid; j < I.z; j += nwarps) {
-            if (K == 8)
-                filter_ref<STEP, K, true, LPS>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                               B.tab_nsx, A);
-            else
-                filter_ref<STEP, K, true, LPS>(V->h, V->t, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                               B.tab_nsx, A);
+            filter_ref<STEP, K, true, LPS>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
+                                           B.tab_nsx, A);
             __syncwarp();
         }
         __syncthreads();
