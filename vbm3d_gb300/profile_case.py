@@ -50,6 +50,7 @@ def main():
                     help="plain form: the deterministic aggregation (vbm3d_set_deterministic)")
     ap.add_argument("--bm-tile", type=int, default=FIXED["bm1_tile"], help="batched block matching: refs per item")
     ap.add_argument("--bm-warps", type=int, default=FIXED["bm1_warps"], help="batched block matching: warps per block")
+    ap.add_argument("--plain", action="store_true", help="with --batch: the clips looped through the plain path")
     ap.add_argument("--filter-tile", type=int, default=FIXED["filter1_tile"], help="batched filtering: refs per item")
     ap.add_argument("--filter-warps", type=int, default=FIXED["filter1_warps"],
                     help="batched filtering: warps per block")
@@ -75,6 +76,13 @@ def main():
         for i, (w, h, f, c, s) in enumerate(batch_specs(scale=a.scale)[:a.batch]):
             _, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)
             clips.append(dict(noisy=torch.from_numpy(noisy).cuda(), sigma=s))
+        if a.plain:
+            for _ in range(a.runs):
+                for c in clips:
+                    vb.run(c["noisy"].clone(), c["sigma"], color_space=True)
+            torch.cuda.synchronize()
+            print("ok")
+            return
         cfg = dict(FIXED, bm1_tile=a.bm_tile, bm2_tile=a.bm_tile, bm1_warps=a.bm_warps, bm2_warps=a.bm_warps,
                    filter1_tile=a.filter_tile, filter2_tile=a.filter_tile, filter1_warps=a.filter_warps,
                    filter2_warps=a.filter_warps)
