@@ -306,7 +306,7 @@ int bm_groups_per_warp(int cls) { return (cls & 1) ? 1 : 2; }
 
 size_t launch_smem(const WorkLaunch& w, int warps)
 {
-    return (w.phase & 1) ? (size_t)(kViewFloats + warps * w.ws) * sizeof(float)
+    return (w.phase & 1) ? (size_t)warps * w.ws * sizeof(float)
                          : (size_t)warps * bm_groups_per_warp(w.cls) * w.ws;
 }
 
@@ -511,9 +511,9 @@ void plan_launches(vbm3d_batch& b)
                 if (class_of(ph, P) != cls) continue;
                 // a full table, or (filtering) transform tables other than the
                 // launch's: next launch
-                const bool next = !(ph & 1) ? (int)w.clips.size() == kTableClips
-                                            : !w.clips.empty() && memcmp(&b.ch[w.clips[0]].t[s], &b.ch[c].t[s],
-                                                                         sizeof(CompactTables)) != 0;
+                const bool next = (int)w.clips.size() == kTableClips ||
+                                  ((ph & 1) && !w.clips.empty() &&
+                                   memcmp(&b.ch[w.clips[0]].t[s], &b.ch[c].t[s], sizeof(CompactTables)) != 0);
                 if (next) {
                     b.work[ph].push_back(w);
                     w.clips.clear();
@@ -571,11 +571,6 @@ int describe(const vbm3d_clip* clips, int nclips, int color_space, vbm3d_batch& 
             h.nrefs[s] = P.nrefs;
         }
         BatchClip& h = b.hc[i];
-        for (int s = 0; s < 2; s++) {
-            h.s[s].v.h = b.ch[i].h[s];
-            h.s[s].v.t = b.ch[i].t[s];
-            h.s[s].L = b.ch[i].L[s];
-        }
         h.in = c.noisy;
         h.fflow = c.fflow;
         h.bflow = c.bflow;
@@ -629,11 +624,22 @@ int allocate(vbm3d_batch& b, cudaStream_t s)
         h.tab_idx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 3]);
         h.tab_nsx = reinterpret_cast<unsigned*>(b.arena + off[5 * i + 4]);
     }
-    // filtering: the transform tables every clip of the launch shares
+    // filtering tables: the transform tables every clip of the launch
+    // shares, the parameters and buffers of each of its clips
     for (int ph = 1; ph < kPhases; ph += 2)
         for (WorkLaunch& w : b.work[ph]) {
-            w.table.assign(sizeof(CompactTables), 0);
-            memcpy(w.table.data(), &b.ch[w.clips[0]].t[ph / 2], sizeof(CompactTables));
+            w.table.assign(sizeof(FilterTable), 0);
+            FilterTable* t = reinterpret_cast<FilterTable*>(w.table.data());
+            t->t = b.ch[w.clips[0]].t[ph / 2];
+            for (size_t i = 0; i < w.clips.size(); i++) {
+                const int c = w.clips[i];
+                t->h[i] = b.ch[c].h[ph / 2];
+                t->pair[i] = b.hc[c].pair;
+                t->noisy[i] = b.hc[c].y;
+                t->basic[i] = b.hc[c].basic;
+                t->tab_idx[i] = b.hc[c].tab_idx;
+                t->tab_nsx[i] = b.hc[c].tab_nsx;
+            }
         }
     // block-matching tables: parameters and buffers of each launch's clips
     for (int ph = 0; ph < kPhases; ph += 2)

@@ -19,20 +19,9 @@ struct CompactTables {
     float cn[kTab];
     float cni[kTab];
 };
-struct FilterView {
-    StepHead h;
-    CompactTables t;
-};
-
-struct ClipStep {
-    FilterView v;
-    Layout L;
-    int pad[4];
-};
 
 // One clip of the batch, in device memory.
 struct BatchClip {
-    ClipStep s[2];
     const float* in;     // the caller's noisy clip
     const float* fflow;  // NULL: zero flow
     const float* bflow;
@@ -45,11 +34,6 @@ struct BatchClip {
     float* out_den;
     unsigned wh, C, color, pad;
 };
-
-// The filtering kernels' shared-memory copy of a clip's FilterView at the
-// start of a block's dynamic shared memory, a 16-byte multiple.
-constexpr int kViewFloats = (int)(((sizeof(FilterView) + 15) & ~size_t(15)) / 4);
-static_assert(sizeof(FilterView) % 4 == 0, "word copies");
 
 // Block matching reads its clips' parameters and buffers from a table
 // passed by value as a __grid_constant__ kernel argument (under the 32 KB
@@ -70,9 +54,22 @@ struct BmTable {
 };
 static_assert(sizeof(BmTable) <= 31 * 1024, "kernel parameter limit");
 
+// Filtering reads the transform tables its launch's clips share and each
+// clip's parameters and buffers from a table of the same kind.
+struct FilterTable {
+    CompactTables t;
+    StepHead h[kTableClips];
+    float* pair[kTableClips];          // interleaved (numerator, denominator)
+    const float* noisy[kTableClips];   // the clip in the working colour space
+    const float* basic[kTableClips];
+    const unsigned* tab_idx[kTableClips];
+    const unsigned* tab_nsx[kTableClips];
+};
+static_assert(sizeof(FilterTable) <= 31 * 1024, "kernel parameter limit");
+
 // A work item is a uint4 (clip, first reference, references, slot): the
-// references lie in one frame of the clip's grid; block matching reads
-// the clip's entries at `slot` of its launch's table.
+// references lie in one frame of the clip's grid; the work kernels read
+// the clip's entries at `slot` of their launch's table.
 
 // Work phases and kernel classes: block matching has one class per
 // (k, C) in {7, 8} x {1, 3}; filtering one per transform table set,

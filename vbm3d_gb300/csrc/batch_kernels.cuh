@@ -8,14 +8,6 @@
 namespace vbm3d {
 namespace batched {
 
-// Block-wide word copy (a clip's parameters into shared memory).
-__device__ __forceinline__ void copy_words(void* dst, const void* src, int bytes)
-{
-    const int* s = reinterpret_cast<const int*>(src);
-    int* d = reinterpret_cast<int*>(dst);
-    for (int i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = __ldg(s + i);
-}
-
 constexpr unsigned kNoItem = 0xffffffffu;
 
 // Work items are taken one ahead: thread 0 claims the block's next item
@@ -39,14 +31,14 @@ __device__ __forceinline__ void claim_item(const uint4* __restrict__ items, unsi
 // w + warps, ...), so at any time a block works on neighbouring reference
 // patches whose search windows and groups overlap in L1, as a block of the
 // plain kernel does.  Block matching reads its clips' parameters from the
-// launch's kernel-argument table (batch.cuh).  Filtering keeps its current
-// clip's scalar parameters in shared memory, reloaded when an item of
-// another clip comes up, and reads the transform tables of its class (the
-// same for every clip of the launch) from its kernel arguments, so each
-// table entry is a constant-bank operand of the transforms' FMAs (k = 8:
-// -7 % to -16 % per launch against tables in shared memory; k = 7, with
-// the DCT passes through their even and odd halves: 96 registers instead
-// of 128, step-2 RGB launches -3.5 % to -7 %).
+// launch's kernel-argument table (batch.cuh), and so does filtering, whose
+// table also holds the transform tables of its class (the same for every
+// clip of the launch): each table entry is a constant-bank operand of the
+// transforms' FMAs (k = 8: -7 % to -16 % per launch against tables in
+// shared memory; k = 7, with the DCT passes through their even and odd
+// halves: 96 registers instead of 128, step-2 RGB launches -3.5 % to
+// -7 %), and the clip's parameters are constant-cache reads instead of
+// shared-memory loads.
 
 // A reference patch takes a group of G lanes, as in bm2_kernel: a warp for
 // three channels, a half warp for one.
@@ -79,30 +71,23 @@ batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ i
 template <int STEP, int K, int LPS>
 __global__ void __launch_bounds__(256, 2)
 batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
-                    unsigned* __restrict__ head, int warp_floats, const __grid_constant__ CompactTables T)
+                    unsigned* __restrict__ head, int warp_floats, const __grid_constant__ FilterTable T)
 {
     extern __shared__ __align__(16) float fsm[];
     __shared__ uint4 s_item[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    FilterView* V = reinterpret_cast<FilterView*>(fsm);
-    float* base = fsm + kViewFloats + (size_t)wid * warp_floats;
-    unsigned cur = kNoItem;
+    float* base = fsm + (size_t)wid * warp_floats;
     claim_item(items, nitems, head, &s_item[0]);
     __syncthreads();
     for (int buf = 0;; buf ^= 1) {
         const uint4 I = s_item[buf];
         if (I.x == kNoItem) break;
         claim_item(items, nitems, head, &s_item[buf ^ 1]);
-        const BatchClip& B = clips[I.x];
-        if (I.x != cur) {
-            copy_words(&V->h, &B.s[STEP - 1].v.h, (int)sizeof(StepHead));
-            __syncthreads();
-            cur = I.x;
-        }
-        const AggTarget A{nullptr, nullptr, B.pair};
+        const int t = (int)I.w;
+        const AggTarget A{nullptr, nullptr, T.pair[t]};
         for (unsigned j = wid; j < I.z; j += nwarps) {
-            filter_ref<STEP, K, true, LPS>(V->h, T, (long long)I.y + j, base, lane, B.y, B.basic, B.tab_idx,
-                                           B.tab_nsx, A);
+            filter_ref<STEP, K, true, LPS>(T.h[t], T.t, (long long)I.y + j, base, lane, T.noisy[t], T.basic[t],
+                                           T.tab_idx[t], T.tab_nsx[t], A);
             __syncwarp();
         }
         __syncthreads();
