@@ -69,9 +69,18 @@ def plain(c, dev, color_space, flows=True):
 
 
 def assert_close(clean, got_b, got_d, want_b, want_d):
+    # basic estimates: within 1e-3 at every value.  Final estimates: the
+    # basic estimates' last bits depend on the order of the aggregation's
+    # float atomics, and a near-tie of step 2's block matching that flips
+    # changes the groups, and so the final values, of the patches involved
+    # (by up to a few units: 3.6 at most on the full-size workloads); on
+    # these small clips that reached 1.3 % of the values in one run of about
+    # fifteen, so the share is bounded at 3 %, the size at 8 and the PSNR
+    # difference at 0.01 dB.  A stale input or a wrong clip parameter moves
+    # most values, by about sigma, and the PSNR.
     assert np.abs(got_b - want_b).max() <= TOL
     d = np.abs(got_d - want_d)
-    assert (d > TOL).mean() < 0.01, (d.max(), (d > TOL).mean())
+    assert (d > TOL).mean() < 0.03 and d.max() < 8.0, (d.max(), (d > TOL).mean())
     assert abs(psnr(clean, got_d) - psnr(clean, want_d)) <= 0.01
     assert abs(psnr(clean, got_b) - psnr(clean, want_b)) <= 0.01
 
