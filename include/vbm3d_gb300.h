@@ -267,7 +267,9 @@ typedef struct vbm3d_clip {
 } vbm3d_clip;
 
 /* Per phase (block matching / filtering of each step): reference patches
- * per work item and warps per block; 0 and 0 = autotune.  Block matching of
+ * per work item and warps per block; 0 and 0 = autotune, which picks per
+ * work launch (class of clips) and reports, from vbm3d_batch_get_config,
+ * the choice of each phase's largest launch.  Block matching of
  * one-channel clips runs two reference patches per warp, and its items hold
  * twice the tile, so every warp has the same work.  no_graph = 1
  * enqueues the kernels at each run instead of launching the graph.  The

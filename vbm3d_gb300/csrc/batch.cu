@@ -192,10 +192,13 @@ struct WorkLaunch {
     unsigned nitems = 0;
     size_t cap = 0;
     int grid = 0;
+    PhaseCfg cfg{0, 0};      // refs per item and warps per block of this launch
 };
 
+// Tuned configurations per batch signature: one per work launch, in phase
+// order (the signature fixes the launches).
 std::mutex g_tune_mu;
-std::map<std::string, vbm3d_batch_config> g_tune_cache;
+std::map<std::string, std::vector<PhaseCfg>> g_tune_cache;
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -291,10 +294,10 @@ int upload_items(WorkLaunch& w, const std::vector<uint4>& v, cudaStream_t s)
     return VBM3D_OK;
 }
 
-int upload_phase(vbm3d_batch& b, int phase, int tile, int stride, cudaStream_t s)
+int upload_phase(vbm3d_batch& b, int phase, int stride, cudaStream_t s)
 {
     for (WorkLaunch& w : b.work[phase]) {
-        int rc = upload_items(w, make_items(b, w, tile, stride), s);
+        int rc = upload_items(w, make_items(b, w, w.cfg.tile, stride), s);
         if (rc) return rc;
     }
     return VBM3D_OK;
@@ -311,8 +314,9 @@ size_t launch_smem(const WorkLaunch& w, int warps)
 }
 
 // Grid of a launch: resident blocks per SM x SMs.
-int launch_grid(const vbm3d_batch& b, const WorkLaunch& w, int warps, int& grid)
+int launch_grid(const vbm3d_batch& b, const WorkLaunch& w, int& grid)
 {
+    const int warps = w.cfg.warps;
     const void* k = work_kernel(w.phase, w.cls);
     const size_t smem = launch_smem(w, warps);
     BCK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -324,18 +328,19 @@ int launch_grid(const vbm3d_batch& b, const WorkLaunch& w, int warps, int& grid)
     return VBM3D_OK;
 }
 
-int phase_grids(vbm3d_batch& b, int phase, int warps)
+int phase_grids(vbm3d_batch& b, int phase)
 {
     for (WorkLaunch& w : b.work[phase]) {
-        int rc = launch_grid(b, w, warps, w.grid);
+        int rc = launch_grid(b, w, w.grid);
         if (rc) return rc;
     }
     return VBM3D_OK;
 }
 
 // One work launch, pulling from queue head h.
-cudaError_t launch_work(const vbm3d_batch& b, const WorkLaunch& w, int warps, unsigned* h, cudaStream_t s)
+cudaError_t launch_work(const vbm3d_batch& b, const WorkLaunch& w, unsigned* h, cudaStream_t s)
 {
+    const int warps = w.cfg.warps;
     if (!w.nitems) return cudaSuccess;
     const BatchClip* clips = b.d_clips;
     const uint4* items = w.d_items;
@@ -347,10 +352,10 @@ cudaError_t launch_work(const vbm3d_batch& b, const WorkLaunch& w, int warps, un
 }
 
 // The launches of one phase, launch i pulling from heads[i].
-cudaError_t launch_phase(const vbm3d_batch& b, int phase, int warps, unsigned* heads, cudaStream_t s)
+cudaError_t launch_phase(const vbm3d_batch& b, int phase, unsigned* heads, cudaStream_t s)
 {
     for (size_t i = 0; i < b.work[phase].size(); i++) {
-        cudaError_t e = launch_work(b, b.work[phase][i], warps, heads + i, s);
+        cudaError_t e = launch_work(b, b.work[phase][i], heads + i, s);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -380,7 +385,7 @@ int enqueue_all(const vbm3d_batch& b, cudaStream_t s)
     BCK(cudaMemsetAsync(b.d_heads, 0, (b.nheads / 2) * sizeof(unsigned), s));
     BCK(launch_elementwise(b, 0, s));
     for (int ph = 0; ph < kPhases; ph++) {
-        BCK(launch_phase(b, ph, b.cfg[ph].warps, phase_heads(b, ph, false), s));
+        BCK(launch_phase(b, ph, phase_heads(b, ph, false), s));
         if (ph == 1) BCK(launch_elementwise(b, 1, s));
     }
     BCK(launch_elementwise(b, 2, s));
@@ -401,31 +406,51 @@ std::string signature(const vbm3d_batch& b)
     return sig;
 }
 
-// Times one candidate configuration of a phase on the sampled items
-// uploaded for it, in ms.
-int time_candidate(vbm3d_batch& b, int phase, const PhaseCfg& c, float& ms)
+// Times one candidate configuration (set in every launch of the phase) on
+// the sampled items uploaded for it: ms[i] for launch i, in ms.
+int time_candidate(vbm3d_batch& b, int phase, std::vector<float>& ms)
 {
-    int rc = phase_grids(b, phase, c.warps);
+    int rc = phase_grids(b, phase);
     if (rc) return rc;
-    cudaEvent_t e0, e1;
-    BCK(cudaEventCreate(&e0));
-    BCK(cudaEventCreate(&e1));
+    const size_t n = b.work[phase].size();
+    std::vector<cudaEvent_t> ev(n + 1);
+    for (auto& e : ev) BCK(cudaEventCreate(&e));
     unsigned* h = phase_heads(b, phase, true);
-    BCK(cudaMemsetAsync(h, 0, b.work[phase].size() * sizeof(unsigned), b.cs));
-    BCK(cudaEventRecord(e0, b.cs));
-    BCK(launch_phase(b, phase, c.warps, h, b.cs));
-    BCK(cudaEventRecord(e1, b.cs));
-    BCK(cudaEventSynchronize(e1));
-    BCK(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    BCK(cudaMemsetAsync(h, 0, n * sizeof(unsigned), b.cs));
+    for (size_t i = 0; i < n; i++) {
+        BCK(cudaEventRecord(ev[i], b.cs));
+        BCK(launch_work(b, b.work[phase][i], h + i, b.cs));
+    }
+    BCK(cudaEventRecord(ev[n], b.cs));
+    BCK(cudaEventSynchronize(ev[n]));
+    ms.assign(n, 0.f);
+    for (size_t i = 0; i < n; i++) BCK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+    for (auto& e : ev) cudaEventDestroy(e);
     return VBM3D_OK;
+}
+
+// The configuration reported for a phase: that of its launch with the most
+// reference patches.
+PhaseCfg phase_cfg(const vbm3d_batch& b, int phase)
+{
+    PhaseCfg c{0, 0};
+    long long most = -1;
+    for (const WorkLaunch& w : b.work[phase]) {
+        long long n = 0;
+        for (int i : w.clips) n += b.ch[i].nrefs[phase / 2];
+        if (n > most) {
+            most = n;
+            c = w.cfg;
+        }
+    }
+    return c;
 }
 
 // Uploads every phase's work items and sizes its grids.  Phases whose
 // configuration is not fixed (by the caller or the cache) are first tuned
 // during one eager pass over the batch, each on a sample of its items with
-// the inputs of the previous phases in place.
+// the inputs of the previous phases in place; every launch (class) of the
+// phase keeps the candidate that was fastest for it.
 int tune_and_prepare(vbm3d_batch& b, const bool fixed[kPhases])
 {
     // candidates (refs per item, warps per block): one or two references
@@ -442,33 +467,36 @@ int tune_and_prepare(vbm3d_batch& b, const bool fixed[kPhases])
     }
     for (int ph = 0; ph < kPhases; ph++) {
         int rc;
+        std::vector<WorkLaunch>& ws = b.work[ph];
         if (!fixed[ph]) {
-            float best = 3.0e38f;
-            PhaseCfg pick{0, 0};
+            std::vector<float> best(ws.size(), 3.0e38f), ms;
+            std::vector<PhaseCfg> pick(ws.size(), PhaseCfg{0, 0});
             const PhaseCfg* cand = (ph & 1) ? cand_f : cand_bm;
             int uploaded = 0;
             for (int ci = 0; ci < ((ph & 1) ? kCandF : kCandBm); ci++) {
                 const PhaseCfg c = cand[ci];
-                float ms = 0.f;
+                for (WorkLaunch& w : ws) w.cfg = c;
                 if (c.tile != uploaded) {
-                    if ((rc = upload_phase(b, ph, c.tile, kSample, s))) return rc;
+                    if ((rc = upload_phase(b, ph, kSample, s))) return rc;
                     uploaded = c.tile;
-                    if ((rc = time_candidate(b, ph, c, ms))) return rc;  // warm-up on the same sample
+                    if ((rc = time_candidate(b, ph, ms))) return rc;  // warm-up on the same sample
                 }
-                if ((rc = time_candidate(b, ph, c, ms))) return rc;
-                if (ms < best) {
-                    best = ms;
-                    pick = c;
-                }
+                if ((rc = time_candidate(b, ph, ms))) return rc;
+                for (size_t i = 0; i < ws.size(); i++)
+                    if (ms[i] < best[i]) {
+                        best[i] = ms[i];
+                        pick[i] = c;
+                    }
             }
-            b.cfg[ph] = pick;
+            for (size_t i = 0; i < ws.size(); i++) ws[i].cfg = pick[i];
             // the sampled filter runs added into the accumulators
             if (ph & 1) BCK(cudaMemsetAsync(b.arena, 0, b.pair_bytes, s));
         }
-        if ((rc = upload_phase(b, ph, b.cfg[ph].tile, 1, s))) return rc;
-        if ((rc = phase_grids(b, ph, b.cfg[ph].warps))) return rc;
+        b.cfg[ph] = phase_cfg(b, ph);
+        if ((rc = upload_phase(b, ph, 1, s))) return rc;
+        if ((rc = phase_grids(b, ph))) return rc;
         if (any) {
-            BCK(launch_phase(b, ph, b.cfg[ph].warps, phase_heads(b, ph, false), s));
+            BCK(launch_phase(b, ph, phase_heads(b, ph, false), s));
             if (ph == 1) BCK(launch_elementwise(b, 1, s));
         }
     }
@@ -745,21 +773,21 @@ int vbm3d_batch_create(const vbm3d_clip* clips, int nclips, int color_space, con
         release(b);
         return cuda_fail(e, "cudaStreamSynchronize");
     }
+    // per phase: the caller's configuration for all its launches, else the
+    // cached per-launch choices of an earlier batch of the same signature,
+    // else tuning
     bool fixed[kPhases];
     const std::string sig = signature(*b);
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tune_cache.find(sig);
+        size_t k = 0;
         for (int ph = 0; ph < kPhases; ph++) {
-            if (b->cfg[ph].tile == 0 && it != g_tune_cache.end()) {
-                const vbm3d_batch_config& c = it->second;
-                const int v[kPhases][2] = {{c.bm1_tile, c.bm1_warps},
-                                           {c.filter1_tile, c.filter1_warps},
-                                           {c.bm2_tile, c.bm2_warps},
-                                           {c.filter2_tile, c.filter2_warps}};
-                b->cfg[ph] = PhaseCfg{v[ph][0], v[ph][1]};
+            fixed[ph] = b->cfg[ph].tile != 0 || it != g_tune_cache.end();
+            for (WorkLaunch& w : b->work[ph]) {
+                w.cfg = b->cfg[ph].tile != 0 ? b->cfg[ph] : it != g_tune_cache.end() ? it->second[k] : PhaseCfg{0, 0};
+                k++;
             }
-            fixed[ph] = b->cfg[ph].tile != 0;
         }
     }
     const auto t0 = std::chrono::steady_clock::now();
@@ -770,9 +798,10 @@ int vbm3d_batch_create(const vbm3d_clip* clips, int nclips, int color_space, con
     b->tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
-        vbm3d_batch_config c;
-        config_of(*b, &c);
-        g_tune_cache[sig] = c;
+        std::vector<PhaseCfg> v;
+        for (int ph = 0; ph < kPhases; ph++)
+            for (const WorkLaunch& w : b->work[ph]) v.push_back(w.cfg);
+        g_tune_cache[sig] = v;
     }
     if (b->graph) {
         cudaGraph_t g = nullptr;
@@ -831,7 +860,7 @@ int vbm3d_batch_profile(vbm3d_batch* b, void* stream, vbm3d_batch_launch* out, i
         for (size_t j = 0; j < b->work[ph].size(); j++, i++) {
             const WorkLaunch& w = b->work[ph][j];
             BCK(cudaEventRecord(ev[i], s));
-            BCK(launch_work(*b, w, b->cfg[ph].warps, heads + j, s));
+            BCK(launch_work(*b, w, heads + j, s));
             BCK(cudaEventRecord(ev[i + 1], s));
             vbm3d_batch_launch& o = out[i];
             memset(&o, 0, sizeof o);
@@ -842,8 +871,8 @@ int vbm3d_batch_profile(vbm3d_batch* b, void* stream, vbm3d_batch_launch* out, i
             o.clips = (int)w.clips.size();
             o.items = w.nitems;
             for (int c : w.clips) o.refs += (unsigned long long)b->ch[c].nrefs[ph / 2];
-            o.tile = b->cfg[ph].tile;
-            o.warps = b->cfg[ph].warps;
+            o.tile = w.cfg.tile;
+            o.warps = w.cfg.warps;
             o.grid = w.grid;
         }
         if (ph == 1) BCK(launch_elementwise(*b, 1, s));

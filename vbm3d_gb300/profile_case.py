@@ -51,6 +51,7 @@ def main():
     ap.add_argument("--bm-tile", type=int, default=FIXED["bm1_tile"], help="batched block matching: refs per item")
     ap.add_argument("--bm-warps", type=int, default=FIXED["bm1_warps"], help="batched block matching: warps per block")
     ap.add_argument("--plain", action="store_true", help="with --batch: the clips looped through the plain path")
+    ap.add_argument("--tuned", action="store_true", help="with --batch: the autotuner's configuration")
     ap.add_argument("--filter-tile", type=int, default=FIXED["filter1_tile"], help="batched filtering: refs per item")
     ap.add_argument("--filter-warps", type=int, default=FIXED["filter1_warps"],
                     help="batched filtering: warps per block")
@@ -86,13 +87,13 @@ def main():
         cfg = dict(FIXED, bm1_tile=a.bm_tile, bm2_tile=a.bm_tile, bm1_warps=a.bm_warps, bm2_warps=a.bm_warps,
                    filter1_tile=a.filter_tile, filter2_tile=a.filter_tile, filter1_warps=a.filter_warps,
                    filter2_warps=a.filter_warps)
-        b = vb.Batch(clips, color_space=True, config=cfg)
+        b = vb.Batch(clips, color_space=True, config=None if a.tuned else cfg)
         for _ in range(a.runs):
             b.run()
         torch.cuda.synchronize()
         for l in b.profile():
-            print("launch phase %d k %d C %d: %d clips, %d refs, %.2f ms" % (l["phase"], l["k"], l["channels"],
-                                                                            l["clips"], l["refs"], l["ms"]))
+            print("launch phase %d k %d C %d: %d clips, %d refs, %d x %d, %.2f ms"
+                  % (l["phase"], l["k"], l["channels"], l["clips"], l["refs"], l["tile"], l["warps"], l["ms"]))
         print("ok")
         return
     _, noisy, _, _ = make_clip(a.width, a.height, a.frames, a.channels, a.sigma, seed=4000, vmax=6.0)
