@@ -276,12 +276,15 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
 // cover: a warp takes them 32 at a time; each lane's entry gives a mask of
 // the lanes (pixels) its patch covers, the transposed masks give each lane
 // the entries of the chunk that cover its pixel, which it adds in key
-// order.  Every lane of the warp calls it.
+// order.  A lane loads the terms of up to kBatch of its entries before it
+// adds them (the same products, added in the same order), so their loads
+// are in flight together.  Every lane of the warp calls it.
 template <int K>
 __device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable& kt, const uint2* list, unsigned T,
                                             const Seg& s, int lane, const float* __restrict__ est,
                                             const float* __restrict__ wts, float (&num)[kMaxC], float (&den)[kMaxC])
 {
+    constexpr int kBatch = 4;
     const int x = s.x0 + lane;
     for (unsigned c0 = 0; c0 < T; c0 += 32) {
         unsigned m = 0;
@@ -290,8 +293,38 @@ __device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable
             const int a = max(lo, 0), b = min(lo + K, 32);
             if (b > a) m = (b - a == 32 ? 0xffffffffu : ((1u << (b - a)) - 1u)) << a;
         }
-        for (unsigned mine = transpose32(m, lane); mine; mine &= mine - 1)
-            add_entry<K>(P, kt, list[c0 + (unsigned)(__ffs(mine) - 1)], x, s.y, est, wts, num, den);
+        for (unsigned mine = transpose32(m, lane); mine;) {
+            float e[kBatch][kMaxC], w[kBatch][kMaxC];
+#pragma unroll
+            for (int q = 0; q < kBatch; q++) {
+#pragma unroll
+                for (int c = 0; c < kMaxC; c++) e[q][c] = w[q][c] = 0.f;
+                if (mine) {
+                    const uint2 en = list[c0 + (unsigned)(__ffs(mine) - 1)];
+                    mine &= mine - 1;
+                    // the pixel is covered: column x - px in [0, K)
+                    const int px = (int)(en.y & 0xffffu), py = (int)(en.y >> 16);
+                    const int pq = (s.y - py) * K + (x - px);
+                    const size_t r = en.x >> 3, n = en.x & 7u;
+                    const float kai = kt.w[pq];
+#pragma unroll
+                    for (int c = 0; c < kMaxC; c++) {
+                        if (c < P.C) {
+                            e[q][c] = __ldg(est + ((r * P.C + c) * P.N + n) * (K * K) + pq);
+                            w[q][c] = kai * __ldg(wts + r * P.C + c);
+                        }
+                    }
+                }
+            }
+            // adding 0 to a sum leaves it unchanged (the sums are never -0)
+#pragma unroll
+            for (int q = 0; q < kBatch; q++)
+#pragma unroll
+                for (int c = 0; c < kMaxC; c++) {
+                    num[c] = num[c] + e[q][c];
+                    den[c] = den[c] + w[q][c];
+                }
+        }
     }
 }
 
