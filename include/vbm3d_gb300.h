@@ -151,7 +151,7 @@ int vbm3d_gpu_step1_noalloc(const vbm3d_params *prms, const float *noisy,
  * not to vbm3d_gpu_step1_noalloc, the batched form or the linearised form,
  * which always add with atomics.  Costs device memory for the estimates:
  * (reference patches) * C * N * k^2 floats per step (32 GB for step 2 of a
- * 1920x1080x30 RGB clip), and about 1.35x the time of the atomic path. */
+ * 1920x1080x30 RGB clip), and about 1.15x the time of the atomic path. */
 int vbm3d_set_deterministic(int on);
 int vbm3d_get_deterministic(void);
 

@@ -36,7 +36,7 @@ namespace {
 
 constexpr int kSegW = 32;          // pixels per segment: a warp, lane = pixel
 constexpr int kGatherWarps = 4;
-constexpr int kWarpCap = 1024;     // entries a warp sorts in shared memory
+constexpr int kWarpCap = 512;      // entries a warp sorts in shared memory
 constexpr int kBlockCap = 16384;   // entries an overflow block sorts
 constexpr int kBigThreads = 512;
 constexpr int kScanItems = 4;      // per thread
@@ -210,8 +210,18 @@ __device__ __forceinline__ unsigned seg_total(const StepHead& P, const Seg& s, c
     return T;
 }
 
+// Index of list element e: PAD inserts one element after every 16, so that
+// the sorting network's accesses of a warp (stride-s pairs of 8-byte
+// elements) spread over the 32 banks.
+template <bool PAD>
+__device__ __forceinline__ int lix(int e)
+{
+    return PAD ? e + (e >> 4) : e;
+}
+
 // Copies the segment's entries into list[0 .. T) with the `nthreads`
 // threads of index `tid`.
+template <bool PAD>
 __device__ __forceinline__ void seg_collect(const StepHead& P, const Seg& s, const unsigned* __restrict__ off,
                                             const uint2* __restrict__ ent, uint2* list, int tid, int nthreads)
 {
@@ -219,15 +229,17 @@ __device__ __forceinline__ void seg_collect(const StepHead& P, const Seg& s, con
     for (int py = s.py0; py <= s.py1; py++) {
         unsigned a, b;
         seg_range(P, s, py, off, a, b);
-        for (unsigned j = (unsigned)tid; j < b - a; j += (unsigned)nthreads) list[o + j] = ent[a + j];
+        for (unsigned j = (unsigned)tid; j < b - a; j += (unsigned)nthreads) list[lix<PAD>((int)(o + j))] = ent[a + j];
         o += b - a;
     }
 }
 
+template <bool PAD>
 __device__ __forceinline__ void cmp_swap(uint2* list, int i, int size, int stride)
 {
-    const int lo = ((i & ~(stride - 1)) << 1) | (i & (stride - 1)), hi = lo + stride;
-    const bool up = (lo & size) == 0;
+    const int lo0 = ((i & ~(stride - 1)) << 1) | (i & (stride - 1));
+    const bool up = (lo0 & size) == 0;
+    const int lo = lix<PAD>(lo0), hi = lix<PAD>(lo0 + stride);
     const uint2 a = list[lo], b = list[hi];
     if ((a.x > b.x) == up) {
         list[lo] = b;
@@ -279,7 +291,7 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
 // order.  A lane loads the terms of up to kBatch of its entries before it
 // adds them (the same products, added in the same order), so their loads
 // are in flight together.  Every lane of the warp calls it.
-template <int K>
+template <int K, bool PAD>
 __device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable& kt, const uint2* list, unsigned T,
                                             const Seg& s, int lane, const float* __restrict__ est,
                                             const float* __restrict__ wts, float (&num)[kMaxC], float (&den)[kMaxC])
@@ -289,7 +301,7 @@ __device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable
     for (unsigned c0 = 0; c0 < T; c0 += 32) {
         unsigned m = 0;
         if (c0 + lane < T) {
-            const int lo = (int)(list[c0 + lane].y & 0xffffu) - s.x0;  // first covered lane (may be < 0)
+            const int lo = (int)(list[lix<PAD>((int)c0 + lane)].y & 0xffffu) - s.x0;  // first covered lane (may be < 0)
             const int a = max(lo, 0), b = min(lo + K, 32);
             if (b > a) m = (b - a == 32 ? 0xffffffffu : ((1u << (b - a)) - 1u)) << a;
         }
@@ -300,7 +312,7 @@ __device__ __forceinline__ void walk_sorted(const StepHead& P, const KaiserTable
 #pragma unroll
                 for (int c = 0; c < kMaxC; c++) e[q][c] = w[q][c] = 0.f;
                 if (mine) {
-                    const uint2 en = list[c0 + (unsigned)(__ffs(mine) - 1)];
+                    const uint2 en = list[lix<PAD>((int)c0 + __ffs(mine) - 1)];
                     mine &= mine - 1;
                     // the pixel is covered: column x - px in [0, K)
                     const int px = (int)(en.y & 0xffffu), py = (int)(en.y >> 16);
@@ -348,7 +360,7 @@ det_gather(const StepHead P, const KaiserTable kt, const float* __restrict__ est
            const unsigned* __restrict__ off, const uint2* __restrict__ ent, float* __restrict__ pair,
            unsigned* __restrict__ ovf, long long nseg)
 {
-    __shared__ uint2 lists[kGatherWarps][kWarpCap];
+    __shared__ uint2 lists[kGatherWarps][kWarpCap + kWarpCap / 16];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long seg = (long long)blockIdx.x * kGatherWarps + wid;
     if (seg >= nseg) return;
@@ -359,19 +371,19 @@ det_gather(const StepHead P, const KaiserTable kt, const float* __restrict__ est
         return;
     }
     uint2* list = lists[wid];
-    seg_collect(P, s, off, ent, list, lane, 32);
+    seg_collect<true>(P, s, off, ent, list, lane, 32);
     int M = 32;
     while (M < (int)T) M <<= 1;
-    for (int j = (int)T + lane; j < M; j += 32) list[j] = make_uint2(kNoKey, 0u);
+    for (int j = (int)T + lane; j < M; j += 32) list[lix<true>(j)] = make_uint2(kNoKey, 0u);
     __syncwarp();
     for (int size = 2; size <= M; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int i = lane; i < M / 2; i += 32) cmp_swap(list, i, size, stride);
+            for (int i = lane; i < M / 2; i += 32) cmp_swap<true>(list, i, size, stride);
             __syncwarp();
         }
     float num[kMaxC] = {0.f, 0.f, 0.f}, den[kMaxC] = {0.f, 0.f, 0.f};
     const int x = s.x0 + lane;
-    walk_sorted<K>(P, kt, list, T, s, lane, est, wts, num, den);
+    walk_sorted<K, true>(P, kt, list, T, s, lane, est, wts, num, den);
     seg_write<K>(P, s, x, num, den, pair);
 }
 
@@ -393,18 +405,18 @@ det_gather_big(const StepHead P, const KaiserTable kt, const float* __restrict__
         const int x = s.x0 + lane;
         float num[kMaxC] = {0.f, 0.f, 0.f}, den[kMaxC] = {0.f, 0.f, 0.f};
         if (T <= (unsigned)kBlockCap) {
-            seg_collect(P, s, off, ent, blist, threadIdx.x, blockDim.x);
+            seg_collect<false>(P, s, off, ent, blist, threadIdx.x, blockDim.x);
             int M = 32;
             while (M < (int)T) M <<= 1;
             for (int j = (int)T + threadIdx.x; j < M; j += blockDim.x) blist[j] = make_uint2(kNoKey, 0u);
             __syncthreads();
             for (int size = 2; size <= M; size <<= 1)
                 for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (int i = threadIdx.x; i < M / 2; i += blockDim.x) cmp_swap(blist, i, size, stride);
+                    for (int i = threadIdx.x; i < M / 2; i += blockDim.x) cmp_swap<false>(blist, i, size, stride);
                     __syncthreads();
                 }
             if (threadIdx.x < 32) {
-                walk_sorted<K>(P, kt, blist, T, s, lane, est, wts, num, den);
+                walk_sorted<K, false>(P, kt, blist, T, s, lane, est, wts, num, den);
                 seg_write<K>(P, s, x, num, den, pair);
             }
             __syncthreads();
