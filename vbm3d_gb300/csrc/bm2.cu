@@ -60,7 +60,9 @@ cudaError_t launch_bm2(const StepParams& P, const float* vid, const float* fflow
 {
     const Layout L = bm2_layout(P);
     if (!L.warp_bytes) return cudaErrorInvalidValue;
-    const int warps = 4;
+    // one-channel k = 7 patches: 16 per block (eight warps of two), whose
+    // staged windows overlap in L1; otherwise 4 warps
+    const int warps = (P.C == 1 && P.k == 7) ? 8 : 4;
     cudaError_t e = cudaSuccess;
 #define VBM3D_BM2(KV, CV)                                                                                  \
     if (P.k == KV && P.C == CV) {                                                                          \

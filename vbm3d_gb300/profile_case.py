@@ -78,10 +78,18 @@ def main():
             _, noisy, _, _ = make_clip(w, h, f, c, s, 4000 + i)
             clips.append(dict(noisy=torch.from_numpy(noisy).cuda(), sigma=s))
         if a.plain:
+            times = []
             for _ in range(a.runs):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
                 for c in clips:
                     vb.run(c["noisy"].clone(), c["sigma"], color_space=True)
-            torch.cuda.synchronize()
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            if a.runs > 1:
+                print("plain loop over %d clips: %.2f ms per run (median of %d)"
+                      % (len(clips), sorted(times[1:])[len(times[1:]) // 2], a.runs - 1))
             print("ok")
             return
         cfg = dict(FIXED, bm1_tile=a.bm_tile, bm2_tile=a.bm_tile, bm1_warps=a.bm_warps, bm2_warps=a.bm_warps,
