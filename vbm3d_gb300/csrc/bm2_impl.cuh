@@ -618,9 +618,29 @@ __device__ void stage_tiles(const StepHead& P, const Smem& S, const float* __res
     // offsets fit 32 bits (W * H * F * C < 2^32).
     const unsigned W = (unsigned)P.W, wh = P.wh;
     const unsigned tiles = smem_addr(S.tiles);
+    // a warp's tiles of at most 16 x 14 (the default windows): lane (column
+    // gl & 15, first row gl >> 4) copies rows y0, y0 + 2, ... of every
+    // channel in one unrolled, predicated sequence (RGB launches -1 %; for
+    // half warps the loop below measured faster)
+    constexpr int kRows = 7;
     for (int w = 0; w < nw; w++) {
         const PWin pwn = S.pw[w];
         const int tw = pwn.ww + K - 1, th = pwn.wh + K - 1;
+        if (G == 32 && tw <= 16 && th <= 2 * kRows) {
+            const int x = g.gl & 15, y0 = g.gl >> 4;
+            if (x < tw) {
+                const float* src = vid + (pwn.base + (unsigned)y0 * W + (unsigned)x);
+                const unsigned dst = tiles + 4u * (unsigned)(pwn.tile + y0 * pitch + x);
+#pragma unroll
+                for (int c = 0; c < C; c++)
+#pragma unroll
+                    for (int i = 0; i < kRows; i++)
+                        if (y0 + 2 * i < th)
+                            cp_async4s_nc(dst + 4u * (unsigned)(c * plane + 2 * i * pitch),
+                                          src + ((unsigned)c * wh + 2u * (unsigned)i * W));
+            }
+            continue;
+        }
         int x0 = g.gl, ystep = 1, y0 = 0, xstep = G;
         if (G == 32 && tw <= 16) {
             x0 = g.gl & 15;

@@ -194,6 +194,13 @@ __device__ __forceinline__ void cp_async4s(unsigned dst, const float* src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
+// The same copy without a compiler memory barrier, for loops that issue
+// only copies: the wait that follows them (cp_async_wait_all) is the
+// barrier that orders the tiles' reads after the copies.
+__device__ __forceinline__ void cp_async4s_nc(unsigned dst, const float* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src));
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 struct Pair {
