@@ -345,10 +345,10 @@ def fp32_peak(dev, clocks):
 # DRAM bytes (read + write) per reference patch of the batched step-2 block
 # matching of the RGB k = 7 clips: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of batch_bm_kernel<2, 7, 3, 32> on the small case
-# (python -m vbm3d_gb300.profile_case --batch 16 --scale 0.5: 112.2 MB +
-# 24.5 MB for 973 383 reference patches), scaled by the launch's reference
+# (python -m vbm3d_gb300.profile_case --batch 16 --scale 0.5: 111.7 MB +
+# 24.2 MB for 973 383 reference patches), scaled by the launch's reference
 # patches.
-BM2_DRAM_BYTES_PER_REF = 137.0
+BM2_DRAM_BYTES_PER_REF = 139.7
 
 
 def timed(stream, fn, steps):
