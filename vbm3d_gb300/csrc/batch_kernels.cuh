@@ -68,8 +68,12 @@ batch_bm_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ i
     }
 }
 
+// Registers: the four-lanes-per-slice kernels (one-channel groups) at 96,
+// which holds 5 blocks of 4 warps per SM (their step-2 k = 7 launch -4.7 %
+// against the 116 registers the compiler takes with room for 128); the
+// one-slice-per-lane kernels need up to 128.
 template <int STEP, int K, int LPS>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __maxnreg__(LPS == 4 ? 96 : 128)
 batch_filter_kernel(const BatchClip* __restrict__ clips, const uint4* __restrict__ items, unsigned nitems,
                     unsigned* __restrict__ head, int warp_floats, const __grid_constant__ FilterTable T)
 {
