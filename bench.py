@@ -519,6 +519,11 @@ def run_gpu(args):
                                       "the small case (profile_case --batch 16 --scale 0.5), x the launch's "
                                       "reference patches",
                     "peak_source": peak_src,
+                    # the exact-order sums issue a packed subtract, FMA square and add per two
+                    # candidate-terms: their issue ceiling is half the FMA peak
+                    "exact_order_ceiling": {"peak": round(peak / 2, 1), "frac": round(2 * achieved / peak, 4),
+                                            "what": "3 packed f32x2 ops per 2 candidate-terms (sub, fma square, "
+                                                    "add in the reference's order): half the FMA rate"},
                     "algorithmic_flops": flops, "distances": n_dist, "refs": bm["refs"], "ms": round(bm["ms"], 2),
                     "share_of_run": round(bm["ms"] / sum(l["ms"] for l in launches), 3),
                     "largest_launch": "phase %d k=%d C=%d, %.1f ms" % (top["phase"], top["k"], top["channels"],
