@@ -932,6 +932,14 @@ inline Layout bm2_layout(const StepHead& P)
     off = align16(off + sizeof(PWin) * 2 * P.Nb);
     off = align16(off + sizeof(unsigned) * 2 * kMaxNb);
     off = align16(off + sizeof(int) * (3 + 2 * kMaxNb));
+    // one-channel patches run two per warp, and the two half warps' shared
+    // loads are one instruction: their workspaces 16 banks apart (stride
+    // = 64 mod 128 bytes) put the second half's window loads, whose 15
+    // addresses per half sit on the banks of the odd-pitch pattern, on
+    // banks the first half's use for two lanes at most, and its 16-byte
+    // reference loads on other banks
+    if (P.C == 1)
+        while ((off & 127) != 64) off += 16;
     if (off > 24 * 1024) return L;
     L.warp_bytes = (int)off;
     return L;
