@@ -548,7 +548,11 @@ void plan_launches(vbm3d_batch& b)
                     w.ws = 0;
                 }
                 w.clips.push_back(c);
-                if (ph & 1) w.ws = std::max(w.ws, (kMaxN + (s == 0 ? 1 : 2) * P.C * P.N * (P.k * P.k + 1) + 3) & ~3);
+                if (ph & 1) {
+                    // slices at the stride of the class's lanes per slice
+                    const int sl = std::max(P.k * P.k + 1, slice_stride(P.k, P.C == 1 ? 4 : 1));
+                    w.ws = std::max(w.ws, (kMaxN + (s == 0 ? 1 : 2) * P.C * P.N * sl + 3) & ~3);
+                }
                 else w.ws = std::max(w.ws, (b.ch[c].L[s].warp_bytes + 15) & ~15);
             }
             if (!w.clips.empty()) b.work[ph].push_back(std::move(w));

@@ -81,6 +81,17 @@ struct StepTables {
 // parameter space).
 struct StepParams : StepHead, StepTables {};
 
+// Slice stride (floats) of a group held in shared memory: k*k | 1 when a
+// lane owns a slice (the lanes' reads of one element fall on distinct
+// banks); with four lanes per slice (one-channel groups: 8 slices x 4
+// lanes) a stride that spreads the row and column passes over the banks
+// (k = 7: 52, no conflict; k = 8: 67, at most 2-way; k*k | 1 gave 2-way and
+// 4-way conflicts).
+__host__ __device__ constexpr int slice_stride(int k, int lps)
+{
+    return lps == 4 ? (k == 7 ? 52 : k == 8 ? 67 : ((k * k) | 1)) : ((k * k) | 1);
+}
+
 // Reference r of the grid, frames outer, then rows, then columns
 // (the loop order of src/vbm3d.cpp:527-538).
 __device__ __forceinline__ void ref_coords(const StepHead& P, long long r, int& x, int& y, int& t)

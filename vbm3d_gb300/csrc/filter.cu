@@ -263,7 +263,8 @@ cudaError_t launch_k_mode(const StepParams& P, const float* noisy, const float* 
                           const unsigned* tab_nsx, const AggTarget& A, long long count, cudaStream_t stream)
 {
     const int warps = 4;
-    const int wf = kMaxN + (STEP == 1 ? 1 : 2) * P.C * P.N * (K * K + 1);
+    constexpr int kSlice = slice_stride(K, LPS) > K * K + 1 ? slice_stride(K, LPS) : K * K + 1;
+    const int wf = kMaxN + (STEP == 1 ? 1 : 2) * P.C * P.N * kSlice;
     const size_t smem = (size_t)warps * wf * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(filter_kernel_k<STEP, K, PAIR, LPS, STORE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -577,17 +577,17 @@ __device__ __forceinline__ float wiener_vector(const float* gn, float* gb, int s
 // 1D transform along the group, shrinkage and the per-channel weights of
 // one group held in shared memory as slices [c][n][k*k] of stride ss; one
 // coefficient vector (c, pq) per lane.
-template <int STEP, int NMAX = 32, int K = 0>
+template <int STEP, int NMAX = 32, int K = 0, int SSK = 0>
 __device__ __forceinline__ void group_1d(const StepHead& P, float* gA, float* gB, int nsx, int ss, int lane,
                                         float* wgt)
 {
     // slices are laid out [c][n][ht][k*k] with stride ss; the coefficient
     // vector (c, ht, pq) runs over n with stride kt*ss.  Its index in the
     // reference's group_3D is pq + ht*k*k, so the group DC is pq = ht = 0.
-    // K > 0: the register-resident path's compile-time k (kt == 1, slice
-    // stride (k*k) | 1 as filter_ref lays the slices out)
+    // K > 0: the register-resident path's compile-time k (kt == 1) and
+    // slice stride SSK
     const int k2 = K ? K * K : P.k * P.k, kt = K ? 1 : P.kt, k2t = k2 * kt, C = P.C;
-    const int ns = K ? ((K * K) | 1) : kt * ss;
+    const int ns = K ? SSK : kt * ss;
     if (K) ss = ns;
     float acc[kMaxC] = {0.f, 0.f, 0.f};
     for (int v = lane; v < C * k2t; v += 32) {
@@ -652,8 +652,7 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
                                            const unsigned* __restrict__ tab_idx, const unsigned* __restrict__ tab_nsx,
                                            const AggTarget& A)
 {
-    // odd slice stride: a lane per slice reads on distinct banks
-    constexpr int K2 = K * K, SS = K2 | 1;
+    constexpr int K2 = K * K, SS = slice_stride(K, LPS);
     const int C = P.C;
     unsigned* idx = reinterpret_cast<unsigned*>(base);
     float* gA = base + kMaxN;               // noisy group
@@ -689,7 +688,7 @@ __device__ __forceinline__ void filter_ref(const StepHead& P, const TT& T, long 
     }
 
     float wgt[kMaxC];
-    group_1d<STEP, 8, K>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
+    group_1d<STEP, 8, K, SS>(P, gA, gB, nsx, SS, lane, wgt);  // the host sends N > 8 to the generic kernel
 
     // inverse 2D, as the forward one
     float* ge = STEP == 1 ? gA : gB;
